@@ -1,0 +1,188 @@
+"""Loads libdimgpu.so (the CUDA kernels behind the C ABI of include/dimgpu.h) and declares its signatures.
+
+There is no fallback: if the library is missing or cannot be loaded, importing anything that needs
+it raises.  Build it with ``python -c "import __graft_entry__ as g; g.build()"`` or
+``python -m diploma_research_gb300.build``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libdimgpu.so")
+
+OK = 0
+ERR_INVALID_ARGUMENT = -1
+ERR_CUDA = -2
+ERR_OUT_OF_MEMORY = -3
+ERR_TIMEOUT = -4
+ERR_BREAKDOWN = -5
+ERR_NOT_CONVERGED = -6
+ERR_UNSUPPORTED = -7
+ERR_BAD_INDEX = -8
+
+MEM_HOST = 0
+MEM_DEVICE = 1
+
+CG_FP64 = 0
+CG_MIXED = 1
+
+_lock = threading.Lock()
+_lib = None
+
+
+class csr5_options(ctypes.Structure):
+    _fields_ = [("sigma", ctypes.c_uint32), ("omega", ctypes.c_uint32), ("layout", ctypes.c_int32),
+                ("flags", ctypes.c_uint32)]
+
+
+class csr5_info(ctypes.Structure):
+    _fields_ = [("rows", ctypes.c_uint32), ("cols", ctypes.c_uint32), ("nnz", ctypes.c_uint64),
+                ("sigma", ctypes.c_uint32), ("omega", ctypes.c_uint32), ("layout", ctypes.c_int32),
+                ("desc_word_bytes", ctypes.c_uint32), ("tile_count", ctypes.c_uint64),
+                ("tile_desc_offset_len", ctypes.c_uint64), ("tail_partition_start", ctypes.c_uint32),
+                ("empty_rows", ctypes.c_uint32), ("device_bytes", ctypes.c_uint64)]
+
+
+class cg_params(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("max_it", ctypes.c_int64), ("precision", ctypes.c_int32),
+                ("use_graph", ctypes.c_int32), ("reliable_delta", ctypes.c_double)]
+
+
+class cg_stats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int64), ("reliable_updates", ctypes.c_int64),
+                ("rel_residual", ctypes.c_double), ("recurrence_rel_residual", ctypes.c_double),
+                ("seconds", ctypes.c_double), ("status", ctypes.c_int32)]
+
+
+class DimgpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"dimgpu error {code}: {msg}")
+        self.code = code
+
+
+class BreakdownError(DimgpuError):
+    pass
+
+
+class NotConvergedError(DimgpuError):
+    pass
+
+
+class DeviceTimeoutError(DimgpuError):
+    pass
+
+
+_vp = ctypes.c_void_p
+_u32 = ctypes.c_uint32
+_u64 = ctypes.c_uint64
+_i32 = ctypes.c_int32
+_f64 = ctypes.c_double
+
+# name -> argtypes (all functions return int unless noted)
+_SIGNATURES = {
+    "dimgpu_csr5_from_csr": [_u32, _u32, _u64, _vp, _vp, _vp, ctypes.c_int, ctypes.POINTER(csr5_options), _vp,
+                             ctypes.POINTER(_vp)],
+    "dimgpu_csr5_destroy": [_vp],
+    "dimgpu_csr5_get_info": [_vp, ctypes.POINTER(csr5_info)],
+    "dimgpu_csr5_export": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "dimgpu_calibrator_create": [_vp, ctypes.POINTER(_vp)],
+    "dimgpu_calibrator_destroy": [_vp],
+    "dimgpu_csr5_spmv": [_vp, _vp, _vp, _vp, _vp],
+    "dimgpu_csr5_spmv_host": [_vp, _vp, _vp],
+    "dimgpu_csr5_spmv_f32": [_vp, _vp, _vp, _vp, _vp],
+    "dimgpu_vec_axpy": [_u64, _f64, _vp, _vp, _vp],
+    "dimgpu_vec_aypx": [_u64, _f64, _vp, _vp, _vp],
+    "dimgpu_vec_set": [_u64, _f64, _vp, _vp],
+    "dimgpu_vec_dot": [_u64, _vp, _vp, ctypes.POINTER(_f64), _vp],
+    "dimgpu_cg_create": [_vp, ctypes.POINTER(cg_params), _vp, ctypes.POINTER(_vp)],
+    "dimgpu_cg_destroy": [_vp],
+    "dimgpu_cg_solve": [_vp, _vp, _vp, ctypes.POINTER(cg_stats), _vp],
+    "dimgpu_cg_solve_host": [_vp, _vp, _vp, ctypes.POINTER(cg_stats)],
+    "dimgpu_version": [],
+}
+
+
+def declared_symbols():
+    """Every entry point include/dimgpu.h declares."""
+    import re
+
+    hdr = os.path.join(os.path.dirname(HERE), "include", "dimgpu.h")
+    with open(hdr) as fh:
+        return re.findall(r"DIMGPU_API\s+(?:const\s+)?\w+\*?\s+\*?(dimgpu_\w+)\(", fh.read())
+
+
+def lib():
+    """The loaded library; raises when it is missing (there is no CPU fallback)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.isfile(LIB_PATH):
+                raise ImportError(f"{LIB_PATH} is missing: build it with diploma_research_gb300.build.build()")
+            L = ctypes.CDLL(LIB_PATH)
+            for name, args in _SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.argtypes = args
+                fn.restype = ctypes.c_int
+            L.dimgpu_last_error_string.argtypes = []
+            L.dimgpu_last_error_string.restype = ctypes.c_char_p
+            _lib = L
+    return _lib
+
+
+def check(rc: int) -> int:
+    if rc == OK:
+        return rc
+    msg = lib().dimgpu_last_error_string().decode(errors="replace")
+    if rc == ERR_INVALID_ARGUMENT:
+        raise ValueError(msg)
+    if rc == ERR_BREAKDOWN:
+        raise BreakdownError(rc, msg)
+    if rc == ERR_NOT_CONVERGED:
+        raise NotConvergedError(rc, msg)
+    if rc == ERR_TIMEOUT:
+        raise DeviceTimeoutError(rc, msg)
+    raise DimgpuError(rc, msg)
+
+
+def device_ptr(a, dtype_str: str | None = None, min_len: int | None = None) -> int:
+    """Device address of an object with __cuda_array_interface__ (torch CUDA tensors, CuPy, ...).
+
+    Checks the element type (numpy-style typestr, e.g. '<f8') and contiguity."""
+    if isinstance(a, int):
+        return a
+    cai = getattr(a, "__cuda_array_interface__", None)
+    if cai is None:
+        raise TypeError("expected a device array (an object exposing __cuda_array_interface__)")
+    if dtype_str is not None and cai["typestr"] != dtype_str:
+        raise TypeError(f"device array has element type {cai['typestr']}, expected {dtype_str}")
+    shape = cai["shape"]
+    strides = cai.get("strides")
+    if strides is not None:
+        expect = int(cai["typestr"][2:])
+        for dim, st in zip(reversed(shape), reversed(strides)):
+            if dim > 1 and st != expect:
+                raise ValueError("device array must be C-contiguous")
+            expect *= dim
+    if min_len is not None:
+        n = 1
+        for d in shape:
+            n *= d
+        if n < min_len:
+            raise ValueError(f"device array has {n} elements, needs {min_len}")
+    return int(cai["data"][0])
+
+
+def is_device_array(a) -> bool:
+    return isinstance(a, int) or hasattr(a, "__cuda_array_interface__")
+
+
+def stream_ptr(stream) -> int:
+    """A cudaStream_t from None, an int, or an object with .cuda_stream (torch.cuda.Stream)."""
+    if stream is None:
+        return 0
+    if isinstance(stream, int):
+        return stream
+    return int(getattr(stream, "cuda_stream"))

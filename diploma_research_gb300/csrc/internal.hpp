@@ -1,0 +1,124 @@
+// internal.hpp -- host-side structures behind the C ABI (include/dimgpu.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/dimgpu.h"
+#include "layout.cuh"
+
+namespace dimgpu {
+
+// Last error message of the calling thread.
+void set_error(const char* fmt, ...);
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define DG_CUDA(call)                                 \
+    do {                                              \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess)                        \
+            return ::dimgpu::cuda_fail(e_, #call);    \
+    } while (0)
+
+#define DG_CHECK(code_expr)            \
+    do {                               \
+        int rc_ = (code_expr);         \
+        if (rc_ != DIMGPU_OK)          \
+            return rc_;                \
+    } while (0)
+
+// Device allocation helpers: return DIMGPU_OK or DIMGPU_ERR_OUT_OF_MEMORY.
+int dev_alloc(void** p, size_t bytes);
+template <typename T>
+int dev_alloc_n(T** p, size_t n) {
+    return dev_alloc(reinterpret_cast<void**>(p), n * sizeof(T) + (n == 0 ? 16 : 0));
+}
+void dev_free(void* p);
+
+// How one SpMV launch covers the tiles: each warp owns a contiguous run of tiles.
+struct spmv_plan {
+    int grid = 1;                  // CTAs
+    int warps_per_cta = 1;
+    uint64_t tiles_per_warp = 0;
+    uint32_t nwarps = 1;           // grid * warps_per_cta (calibrator slots)
+};
+
+}  // namespace dimgpu
+
+struct dimgpu_calibrator {
+    int device = 0;
+    uint32_t nslots = 0;
+    double* cal_val = nullptr;    // [nslots] head partial sum of each warp's first row
+    uint32_t* cal_row = nullptr;  // [nslots] that row, MSB set when the slot is valid
+    double* dot_part = nullptr;   // [nslots + 1] per-warp partials of the fused dot product
+    uint32_t* counter = nullptr;  // CTA completion ticket (reset by the last CTA)
+    uint32_t* status = nullptr;   // device status word (dimgpu::device_status)
+};
+
+struct dimgpu_csr5 {
+    int device = 0;
+    uint32_t rows = 0, cols = 0;
+    uint64_t nnz = 0;
+    uint32_t sigma = 16, omega = 32;
+    int layout = dimgpu::kLayoutDevice;
+    uint64_t tile_count = 0;
+    uint32_t tail_start = 0;
+    uint32_t desc_word_bytes = 4;
+    uint64_t tdo_len = 0;
+    uint32_t n_empty = 0;
+
+    uint32_t* row_ptr = nullptr;   // [rows+1]
+    double* vals = nullptr;        // [nnz] re-ordered
+    uint32_t* col = nullptr;       // [nnz] re-ordered
+    uint32_t* tile_ptr = nullptr;  // [T+1]
+    void* tile_desc = nullptr;     // [T*omega] words
+    uint32_t* tdo_ptr = nullptr;   // [T+1]
+    uint32_t* tdo = nullptr;       // [tdo_len]
+    uint32_t* empty_rows = nullptr;  // [n_empty]
+    float* vals32 = nullptr;       // f32 values in the device layout (built on first f32 use)
+    uint64_t device_bytes = 0;
+
+    dimgpu::spmv_plan plan;
+    dimgpu_calibrator* own_cal = nullptr;
+};
+
+namespace dimgpu {
+
+// convert.cu
+int convert_csr5(dimgpu_csr5* m, const uint32_t* d_row_ptr, const uint32_t* d_col, const double* d_vals,
+                 cudaStream_t stream);
+int ensure_vals32(const dimgpu_csr5* m, cudaStream_t stream);
+
+// spmv.cu
+spmv_plan make_spmv_plan(uint64_t tiles, int sms);
+int prepare_spmv_kernels();
+int calibrator_init(dimgpu_calibrator* c, const dimgpu_csr5* m);
+void calibrator_release(dimgpu_calibrator* c);
+
+struct spmv_epilogue {
+    // Optional CG epilogue, computed by the last CTA: dot = x.y (written to *dot_out) and, when
+    // rr is given, alpha = *rr / dot (written to *alpha_out); a non-positive or non-finite dot sets
+    // kStatusBreakdown and *halt = 1.
+    double* dot_out = nullptr;
+    const double* rr = nullptr;
+    double* alpha_out = nullptr;
+    uint32_t* halt = nullptr;        // when non-null and *halt != 0 on entry, the launch does nothing
+};
+
+int launch_spmv_f64(const dimgpu_csr5* m, const double* x, double* y, dimgpu_calibrator* cal,
+                    const spmv_epilogue& ep, cudaStream_t stream);
+int launch_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calibrator* cal,
+                    const spmv_epilogue& ep, cudaStream_t stream);
+int check_status(dimgpu_calibrator* cal, cudaStream_t stream);
+
+// api.cu: deterministic dot product into device memory (d_part holds 256 partials)
+int dot_device(uint64_t n, const double* a, const double* b, double* d_out, double* d_part, cudaStream_t s);
+
+int device_sm_count(int device);
+
+}  // namespace dimgpu

@@ -1,0 +1,162 @@
+/*
+ * dimgpu.h -- C ABI of the GB300-native CSR5 library (hand-written sm_103a kernels).
+ *
+ * The reference ("dim", rurabori/diploma_research) exposes this hot path as the header-only C++
+ * template dim::mat::csr5<double,16,4,uint32_t> (include/dim/mat/storage_formats/csr5.h:254-881),
+ * the vector helpers of include/dim/vec.h and the CG loops of benchmarks/conjugate_gradient/.  Each
+ * entry point below names the reference interface it replaces.
+ *
+ * Conventions
+ *   - Every function returns an int status: DIMGPU_OK (0) or a negative DIMGPU_ERR_* code; the
+ *     message of the last failure on the calling thread is dimgpu_last_error_string().  Nothing
+ *     throws across this boundary (the reference throws std::invalid_argument, csr5.h:820-821).
+ *   - Pointers are plain pointers.  Functions whose name ends in _host take host memory and copy
+ *     inside the call; all others take device memory of the current device.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = the legacy default stream).
+ *   - A matrix handle is immutable after creation.  Scratch for one SpMV lives in a calibrator
+ *     (the reference's calibrator_t, csr5/calibrator.h); calls that share a calibrator must not
+ *     overlap on the device, calls with different calibrators may.
+ *   - Index type u32 (row offsets, column indices), values f64, as csr5<double,16,4,uint32_t>.
+ */
+#ifndef DIMGPU_H
+#define DIMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define DIMGPU_API __attribute__((visibility("default")))
+#else
+#define DIMGPU_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DIMGPU_OK 0
+#define DIMGPU_ERR_INVALID_ARGUMENT (-1) /* bad shape/pointer/option (std::invalid_argument) */
+#define DIMGPU_ERR_CUDA (-2)             /* a CUDA runtime call failed */
+#define DIMGPU_ERR_OUT_OF_MEMORY (-3)
+#define DIMGPU_ERR_TIMEOUT (-4)          /* a bounded device-side wait expired */
+#define DIMGPU_ERR_BREAKDOWN (-5)        /* CG: s.As <= 0 or not finite (matrix not SPD) */
+#define DIMGPU_ERR_NOT_CONVERGED (-6)    /* CG: max_it reached before the tolerance */
+#define DIMGPU_ERR_UNSUPPORTED (-7)
+#define DIMGPU_ERR_BAD_INDEX (-8)        /* a device-side bounds check failed */
+
+typedef struct dimgpu_csr5 dimgpu_csr5;             /* device CSR5 matrix */
+typedef struct dimgpu_calibrator dimgpu_calibrator; /* scratch of one SpMV at a time */
+typedef struct dimgpu_cg_solver dimgpu_cg_solver;   /* CG workspace + captured CUDA graph */
+
+typedef enum { DIMGPU_MEM_HOST = 0, DIMGPU_MEM_DEVICE = 1 } dimgpu_mem_kind;
+
+/* Element order inside re-ordered tiles (see layout.cuh). */
+typedef enum { DIMGPU_LAYOUT_REFERENCE = 0, DIMGPU_LAYOUT_DEVICE = 1 } dimgpu_layout;
+
+typedef struct {
+    uint32_t sigma;  /* rows per tile column; 0 = 16 */
+    uint32_t omega;  /* lanes per tile: 32 for the device layout, 4 for the reference layout; 0 = 32 */
+    int32_t layout;  /* dimgpu_layout; ignored (device) when omega == 32 */
+    uint32_t flags;  /* reserved, 0 */
+} dimgpu_csr5_options;
+
+typedef struct {
+    uint32_t rows, cols;
+    uint64_t nnz;
+    uint32_t sigma, omega;
+    int32_t layout;
+    uint32_t desc_word_bytes;      /* 4 or 8 */
+    uint64_t tile_count;           /* csr5_info_t::tile_count (csr5.h:289) */
+    uint64_t tile_desc_offset_len; /* tile_desc_offset.size() */
+    uint32_t tail_partition_start; /* csr5::tail_partition_start() (csr5.h:806) */
+    uint32_t empty_rows;           /* empty rows below tail_partition_start */
+    uint64_t device_bytes;         /* HBM held by the handle */
+} dimgpu_csr5_info;
+
+/* ---- matrices --------------------------------------------------------------------------------- */
+
+/* csr5::from_csr (csr5.h:791-803): builds the CSR5 arrays on the device from a CSR matrix held in
+ * host (mem = DIMGPU_MEM_HOST) or device memory.  The handle owns device copies.  opt may be NULL. */
+DIMGPU_API int dimgpu_csr5_from_csr(uint32_t rows, uint32_t cols, uint64_t nnz, const uint32_t* row_ptr,
+                         const uint32_t* col_idx, const double* vals, int mem, const dimgpu_csr5_options* opt,
+                         void* stream, dimgpu_csr5** out);
+
+DIMGPU_API int dimgpu_csr5_destroy(dimgpu_csr5* m);
+
+/* tile_count, tail_partition_start, non_zero_count (csr5.h:289, 806, 880) and sizes. */
+DIMGPU_API int dimgpu_csr5_get_info(const dimgpu_csr5* m, dimgpu_csr5_info* out);
+
+/* Copies the CSR5 arrays (csr5_info_t members, csr5.h:287-294, and csr5::vals/col_idx/row_ptr,
+ * csr5.h:450-453) to host buffers sized from dimgpu_csr5_get_info.  tile_desc receives
+ * tile_count*omega words of desc_word_bytes each.  Any pointer may be NULL to skip that array. */
+DIMGPU_API int dimgpu_csr5_export(const dimgpu_csr5* m, uint32_t* tile_ptr, void* tile_desc, uint32_t* tile_desc_offset_ptr,
+                       uint32_t* tile_desc_offset, double* vals, uint32_t* col_idx, uint32_t* row_ptr);
+
+/* ---- SpMV ------------------------------------------------------------------------------------- */
+
+/* csr5::create_calibrator (csr5.h:809): scratch for one SpMV at a time on this matrix. */
+DIMGPU_API int dimgpu_calibrator_create(const dimgpu_csr5* m, dimgpu_calibrator** out);
+DIMGPU_API int dimgpu_calibrator_destroy(dimgpu_calibrator* c);
+
+/* csr5::spmv(spmv_data_t{x, y, calibrator}) (csr5.h:280-285, 818-829): y := A x.  y is overwritten
+ * (empty rows get 0), so neither a zero-filled y nor a fresh calibrator is needed.  cal may be
+ * NULL (the matrix's own calibrator; then calls on this matrix must not overlap).  x has cols
+ * elements, y rows elements, both device memory.  Requires a device-layout matrix (omega = 32). */
+DIMGPU_API int dimgpu_csr5_spmv(const dimgpu_csr5* m, const double* x, double* y, dimgpu_calibrator* cal, void* stream);
+
+/* The same product with host x and y: copies x in, multiplies, copies y out, synchronizes. */
+DIMGPU_API int dimgpu_csr5_spmv_host(const dimgpu_csr5* m, const double* x_host, double* y_host);
+
+/* y := A x with f32 values, vectors and row sums (the inner kernel of the mixed-precision CG).
+ * The first call builds an f32 copy of the values inside the handle. */
+DIMGPU_API int dimgpu_csr5_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calibrator* cal, void* stream);
+
+/* ---- vectors (include/dim/vec.h:29-84), device memory ----------------------------------------- */
+
+DIMGPU_API int dimgpu_vec_axpy(uint64_t n, double alpha, const double* x, double* y, void* stream); /* y += a x */
+DIMGPU_API int dimgpu_vec_aypx(uint64_t n, double alpha, const double* x, double* y, void* stream); /* y = x + a y */
+DIMGPU_API int dimgpu_vec_set(uint64_t n, double value, double* y, void* stream);
+/* dot(l, r) (vec.h:78-84); deterministic order; result written to host *out (synchronizes). */
+DIMGPU_API int dimgpu_vec_dot(uint64_t n, const double* l, const double* r, double* out, void* stream);
+
+/* ---- CG (benchmarks/conjugate_gradient/dim_sp/main.cpp:78-141; docs/paper/thesis.tex:2127-2160) */
+
+#define DIMGPU_CG_FP64 0  /* f64 everywhere */
+#define DIMGPU_CG_MIXED 1 /* f32 values/vectors inside, f64 dots, f64 x and reliable f64 residual updates */
+
+typedef struct {
+    double tol;        /* stop when ||r|| <= tol * ||b|| */
+    int64_t max_it;    /* iteration cap */
+    int32_t precision; /* DIMGPU_CG_FP64 or DIMGPU_CG_MIXED */
+    int32_t use_graph; /* 1: whole solve as one CUDA graph with a device-side while loop */
+    double reliable_delta; /* mixed only: replace the residual when it dropped by this factor; 0 = 0.1 */
+} dimgpu_cg_params;
+
+typedef struct {
+    int64_t iterations;      /* CG iterations (inner iterations for the mixed solver) */
+    int64_t reliable_updates; /* f64 residual replacements (mixed) */
+    double rel_residual;      /* ||b - A x|| / ||b|| recomputed in f64 at the end */
+    double recurrence_rel_residual; /* sqrt(r.r)/||b|| of the recurrence at exit */
+    double seconds;           /* device time of the solve (CUDA events) */
+    int32_t status;           /* DIMGPU_OK, _NOT_CONVERGED or _BREAKDOWN */
+} dimgpu_cg_stats;
+
+/* Allocates the CG workspace for matrix m (and, with use_graph, captures the solve graph). */
+DIMGPU_API int dimgpu_cg_create(const dimgpu_csr5* m, const dimgpu_cg_params* params, void* stream, dimgpu_cg_solver** out);
+DIMGPU_API int dimgpu_cg_destroy(dimgpu_cg_solver* s);
+/* Solves A x = b from the initial guess in x (device memory).  Returns the solve status. */
+DIMGPU_API int dimgpu_cg_solve(dimgpu_cg_solver* s, const double* b, double* x, dimgpu_cg_stats* stats, void* stream);
+/* The same with host b and x (copies in and out inside the call). */
+DIMGPU_API int dimgpu_cg_solve_host(dimgpu_cg_solver* s, const double* b_host, double* x_host, dimgpu_cg_stats* stats);
+
+/* ---- diagnostics ------------------------------------------------------------------------------ */
+
+DIMGPU_API const char* dimgpu_last_error_string(void);
+/* Device status word of the last kernel that reported one (0 = none); cleared by this call. */
+DIMGPU_API int dimgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DIMGPU_H */
