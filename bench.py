@@ -1,0 +1,385 @@
+#!/usr/bin/env python3
+"""Benchmark: CG to 1e-10 relative residual on the 3-D 27-point 128^3 stencil (n = 2,097,152,
+nnz = 55,742,968, FP64, diagonal 26 + 1e-3, b = A x*, x* ~ U[-1,1] seed 1), with the FP64 CSR5 SpMV
+roofline beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+One step = one complete CG solve from x0 = 0 on device-resident inputs (the matrix, 702 MB of CSR5
+data, is larger than the 129 MB L2, so no flush is needed between steps).  `value` is FP64 seconds per
+solve; the mixed-precision solve (f32 inner recurrence, f64 reliable updates, same f64 residual
+criterion) is reported beside it.  `e2e` runs the same FP64 solve through the C ABI with host
+buffers (pinned), host<->device copies included.  `roofline` is the FP64 SpMV kernel timed alone
+with CUDA events: algorithmic bytes 12*nnz + 16*n per launch.
+
+--impl reference times the reference's CPU CG (the C restatement of its CSR5 AVX2/OpenMP path,
+oracle/csr5_oracle.c, with all host threads) on the same workload.
+Multi-GPU: replicas only (each rank solves its own copy); max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "CG s to 1e-10 rel. residual, mixed vs FP64 on 1 GB300; SpMV GB/s vs HBM peak"
+WORKLOAD = "stencil27_128"
+TOL = 1e-10
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.isfile(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _profile_traffic():
+    """Per-launch DRAM bytes of the FP64 SpMV from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "spmv_f64_stencil27_128.md")
+    if not os.path.isfile(p):
+        return None
+    with open(p) as fh:
+        for line in fh:
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                try:
+                    return int(float(line.split(":", 1)[1].strip()))
+                except ValueError:
+                    return None
+    return None
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons every 200 ms while alive."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _barrier_max(value: float, ws: int):
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _workload():
+    from diploma_research_gb300.generators import WORKLOADS, rhs
+
+    m = WORKLOADS[WORKLOAD]["build"]()
+    xs, b = rhs(m, WORKLOADS[WORKLOAD]["seed"])
+    return m, xs, b
+
+
+def run_reference(args):
+    """The reference's CPU CG (oracle/csr5_oracle.c restating csr5.h + dim_sp) on all host threads."""
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    import numpy as np
+
+    import oracle
+
+    m, xs, b = _workload()
+    n = m.dimensions.rows
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    o = oracle.OracleCSR5(n, n, m.row_start_offsets, m.col_indices, m.values, 16, 4)
+    convert_s = time.perf_counter() - t0
+    # iterations to converge: one full solve, untimed
+    _, iters, rel = o.cg(b, tol=TOL, nthreads=threads)
+    sample_it = min(iters, 25)
+    for _ in range(args.warmup):
+        o.cg(b, tol=TOL, max_it=sample_it, nthreads=threads)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        o.cg(b, tol=TOL, max_it=sample_it, nthreads=threads)
+        times.append(time.perf_counter() - t)
+    per_it = statistics.mean(times) / sample_it
+    value = per_it * iters
+    sample = (f"{sample_it} CG iterations per step on the full {WORKLOAD} system, scaled to the {iters} iterations "
+              f"the same CPU CG needs to reach {TOL:g} (one full untimed solve, rel. residual {rel:.2e})")
+    out = {"metric": METRIC, "value": value, "unit": "s", "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(times) * 1e3,
+           "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"{WORKLOAD}: 3-D 27-point stencil 128^3, n={n}, nnz={m.nnz}, CG to {TOL:g}",
+                      "global_batch": 1, "parallelism": "cpu-openmp"},
+           "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "iterations": iters, "convert_s": convert_s}
+    print(json.dumps(out))
+    return 0
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo", init_method="env://")
+    torch.cuda.set_device(local)
+    from diploma_research_gb300 import build as B
+
+    B.build()
+    from diploma_research_gb300.cg import CGSolver
+    from diploma_research_gb300.csr5 import csr5
+
+    m, xs, b = _workload()
+    n, nnz = m.dimensions.rows, m.nnz
+    t0 = time.perf_counter()
+    A = csr5.from_csr(m)
+    torch.cuda.synchronize()
+    convert_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream()
+    bd = torch.tensor(b, device="cuda", dtype=torch.float64)
+    xd = torch.zeros(n, device="cuda", dtype=torch.float64)
+    s64 = CGSolver(A, tol=TOL, precision="fp64", stream=stream)
+    smx = CGSolver(A, tol=TOL, precision="mixed", stream=stream)
+
+    def solve(solver):
+        xd.zero_()
+        return solver.solve(bd, xd, stream=stream)[1]
+
+    # ---- FP64 CG: the headline ----
+    for _ in range(args.warmup):
+        res64 = solve(s64)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        iters64 = []
+        for _ in range(args.steps):
+            r = solve(s64)
+            iters64.append(r.iterations)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    sec64 = ev0.elapsed_time(ev1) * 1e-3 / args.steps
+    sec64 = _barrier_max(sec64, ws)
+    err64 = float(np.linalg.norm(xd.cpu().numpy() - xs) / np.linalg.norm(xs))
+    res64 = r
+
+    # ---- mixed-precision CG ----
+    for _ in range(max(1, args.warmup)):
+        resm = solve(smx)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        resm = solve(smx)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    secm = _barrier_max(ev0.elapsed_time(ev1) * 1e-3 / args.steps, ws)
+    errm = float(np.linalg.norm(xd.cpu().numpy() - xs) / np.linalg.norm(xs))
+
+    # ---- FP64 SpMV alone: the dominant kernel, for the roofline ----
+    x1 = torch.tensor(np.random.default_rng(5).uniform(-1, 1, n), device="cuda", dtype=torch.float64)
+    y1 = torch.empty(n, device="cuda", dtype=torch.float64)
+    cal = A.create_calibrator()
+    for _ in range(5):
+        A.spmv(x1, y1, cal, stream=stream)
+    spmv_reps = 50
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(spmv_reps):
+        A.spmv(x1, y1, cal, stream=stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    spmv_s = ev0.elapsed_time(ev1) * 1e-3 / spmv_reps
+    spmv_bytes = 12 * nnz + 16 * n
+    spmv_gbs = spmv_bytes / spmv_s / 1e9
+    peak, peak_kind = _peaks()
+
+    # ---- e2e: the same FP64 solve through the C ABI with pinned host buffers ----
+    bh = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    bh[:] = b
+    xh = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    import ctypes
+
+    from diploma_research_gb300 import _native as N
+
+    st = N.cg_stats()
+    L = N.lib()
+    for _ in range(max(1, args.warmup)):
+        xh[:] = 0
+        N.check(L.dimgpu_cg_solve_host(s64._h, bh.ctypes.data, xh.ctypes.data, ctypes.byref(st)))
+    e2e_t = []
+    for _ in range(args.steps):
+        xh[:] = 0
+        t = time.perf_counter()
+        N.check(L.dimgpu_cg_solve_host(s64._h, bh.ctypes.data, xh.ctypes.data, ctypes.byref(st)))
+        e2e_t.append(time.perf_counter() - t)
+    e2e_s = _barrier_max(statistics.mean(e2e_t), ws)
+
+    # ---- CPU baseline: the reference's CPU CG (C restatement), full solve, rank 0 only ----
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        import oracle
+
+        o = oracle.OracleCSR5(n, n, m.row_start_offsets, m.col_indices, m.values, 16, 4)
+        threads = os.cpu_count() or 1
+        t = time.perf_counter()
+        _, it_cpu, _ = o.cg(b, tol=TOL, nthreads=threads)
+        cpu_s = time.perf_counter() - t
+        cpu = {"value": cpu_s, "unit": "s", "cores": threads, "kind": "port",
+               "sample": f"one full CPU CG solve of {WORKLOAD} to {TOL:g} ({it_cpu} iterations), "
+                         f"oracle/csr5_oracle.c on {threads} host threads"}
+
+    launches_per_solve = 4 + 3 * statistics.mean(iters64)  # init SpMV + init, 3 per iteration, final SpMV + norms
+    clocks = clk.summary()
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": sec64, "unit": "s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": sec64 * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded 27-point stencil, b = A x*, x* ~ U[-1,1] seed 1)",
+            "config": {"workload": f"{WORKLOAD}: 3-D 27-point stencil 128^3, n={n}, nnz={nnz}, CG to {TOL:g} "
+                                   "from x0 = 0, FP64", "global_batch": 1, "seq_len": n,
+                       "parallelism": "replicas" if ws > 1 else "single-gpu",
+                       "l2": "inputs larger than L2 (702 MB of CSR5 data vs 129 MB L2); no flush"},
+            "iterations": res64.iterations, "rel_residual": res64.rel_residual, "rel_error_vs_xstar": err64,
+            "mixed": {"value": secm, "unit": "s", "iterations": resm.iterations,
+                      "reliable_updates": resm.reliable_updates, "rel_residual": resm.rel_residual,
+                      "rel_error_vs_xstar": errm, "speedup_vs_fp64": sec64 / secm, "dtype": "f32 inner / f64"},
+            "spmv": {"seconds": spmv_s, "gbps": spmv_gbs, "bytes_per_launch": spmv_bytes,
+                     "fp64_tflops": 2 * nnz / spmv_s / 1e12},
+            "roofline": {"bound": "hbm", "achieved": spmv_gbs, "peak": peak, "unit": "GB/s",
+                         "frac": spmv_gbs / peak, "traffic": _profile_traffic(), "kernel": "k_spmv<double,16>",
+                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                         else "fallback 6.8 TB/s"},
+            "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
+            "gpu_launches": int(round(launches_per_solve * args.steps)),
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "convert_s": convert_s,
+        }
+        print(json.dumps(out))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def run_spmv_only(args):
+    """A short SpMV-only run (few launches) for profiler captures: 5 warm-up + `steps` launches."""
+    import numpy as np
+    import torch
+
+    from diploma_research_gb300 import build as B
+
+    B.build()
+    from diploma_research_gb300.csr5 import csr5
+
+    m, _, _ = _workload()
+    n, nnz = m.dimensions.rows, m.nnz
+    A = csr5.from_csr(m)
+    stream = torch.cuda.current_stream()
+    x = torch.tensor(np.random.default_rng(5).uniform(-1, 1, n), device="cuda", dtype=torch.float64)
+    y = torch.empty(n, device="cuda", dtype=torch.float64)
+    cal = A.create_calibrator()
+    for _ in range(5):
+        A.spmv(x, y, cal, stream=stream)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        A.spmv(x, y, cal, stream=stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    s = ev0.elapsed_time(ev1) * 1e-3 / args.steps
+    print(json.dumps({"spmv_seconds": s, "gbps": (12 * nnz + 16 * n) / s / 1e9, "nnz": nnz, "n": n}))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="dimgpu", choices=["dimgpu", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--spmv-only", action="store_true", help="few SpMV launches only (for profiler captures)")
+    args = ap.parse_args()
+    if args.spmv_only:
+        return run_spmv_only(args)
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

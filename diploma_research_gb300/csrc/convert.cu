@@ -12,7 +12,7 @@
 //                   segment count + 1 for dirty multi-row tiles (csr5.h:342-361)
 //   k_tdo           tile_desc_offset[ptr + y] = row of each segment, relative to the tile's first
 //                   row (csr5.h:363-397)
-//   k_permute       re-orders every multi-row full tile (csr5.h:463-493) into the chosen layout
+//   k_permute       re-orders full tiles (csr5.h:463-493) into the chosen layout
 //
 // All integer work: the results are bit-identical to the reference's arrays at (16, 4) and to the
 // same construction at omega = 32.  The reference's benign race on tile_desc_offset_ptr.back()
@@ -262,7 +262,9 @@ __global__ void k_permute(const T_* in, T_* out, const uint32_t* tile_ptr, uint6
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < nnz; e += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t t = e / ts;
         uint64_t dst = e;
-        if (t < T && (tile_ptr[t] & ~kDirty) != (tile_ptr[t + 1] & ~kDirty)) {
+        // the reference order leaves single-row tiles alone (csr5.h:466-468); the device orders
+        // re-order every full tile so that pair and quad reads always address the same elements
+        if (t < T && (kind != 0 || (tile_ptr[t] & ~kDirty) != (tile_ptr[t + 1] & ~kDirty))) {
             const uint32_t k = (uint32_t)(e - t * ts);
             const uint32_t c = k / sigma, r = k % sigma;
             const uint32_t p = kind == 0 ? pos_reference(c, r, omega)
@@ -293,14 +295,14 @@ __global__ void k_to_f32(const double* in, float* out, uint64_t n) {
         out[i] = (float)in[i];
 }
 
-// f32 copy of device-layout values: within multi-row tiles the f64 pair order becomes quad order.
+// f32 copy of device-layout values: within every full tile the f64 pair order becomes quad order.
 __global__ void k_vals32_device(const double* vals, float* out, const uint32_t* tile_ptr, uint64_t T, uint64_t nnz,
                                 uint32_t sigma, uint32_t omega) {
     const uint32_t ts = sigma * omega;
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < nnz; e += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t t = e / ts;
         uint64_t src = e;
-        if (t < T && (tile_ptr[t] & ~kDirty) != (tile_ptr[t + 1] & ~kDirty)) {
+        if (t < T) {
             // e is the quad position of element (c, r); read that element from its pair position
             const uint32_t k = (uint32_t)(e - t * ts);
             const uint32_t q = k / (4 * omega), rem = k % (4 * omega);

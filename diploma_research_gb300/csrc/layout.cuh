@@ -10,14 +10,17 @@
 //                        they fit in 32 bits, else u64
 //   tdo_ptr[T+1], tdo[]  tile_desc_offset_ptr / tile_desc_offset: row of each segment of a tile
 //                        that contains empty rows (csr5.h:342-397)
-//   vals[nnz], col[nnz]  the CSR arrays with every full tile that spans more than one row
-//                        re-ordered so that a lane reads its column row by row
+//   vals[nnz], col[nnz]  the CSR arrays with full tiles re-ordered so that a lane reads its column
+//                        row by row
 //
 // Two element orders inside such a tile:
 //   kLayoutReference: element (column c, row r) at r*omega + c            (csr5.h:463-493)
 //   kLayoutDevice:    f64 values in pairs  (r/2)*2*omega + 2c + r%2 (one 16-byte load = 2 rows),
 //                     u32 columns and f32 values in quads (r/4)*4*omega + 4c + r%4 (16 bytes = 4 rows)
-// Fast-track tiles (one row) and the tail (the last nnz mod sigma*omega elements) stay in CSR order.
+// The reference order re-orders only tiles spanning more than one row (single-row "fast-track"
+// tiles stay in CSR order, csr5.h:466-468); the device orders re-order every full tile, so that the
+// pair reads of values and the quad reads of column indices always meet the same elements.  The
+// tail (the last nnz mod sigma*omega elements) stays in CSR order.
 #pragma once
 
 #include <cstdint>

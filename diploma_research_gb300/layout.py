@@ -7,7 +7,8 @@ Within every full tile that spans more than one row, element (column c, row r) -
 * ``(r//2)*2*omega + 2*c + r%2``           device order of f64 values (16-byte pairs)
 * ``(r//4)*4*omega + 4*c + r%4``           device order of u32 column indices and f32 values (quads)
 
-Fast-track tiles (one row) and the tail keep CSR order.
+The reference order leaves single-row (fast-track) tiles in CSR order; the device orders re-order
+every full tile.  The tail keeps CSR order.
 """
 from __future__ import annotations
 
@@ -33,6 +34,11 @@ def multirow_tiles(tile_ptr: np.ndarray) -> np.ndarray:
     return tp[:-1] != tp[1:]
 
 
+def _reordered(tile_ptr, kind):
+    mr = multirow_tiles(tile_ptr)
+    return mr if kind == "ref" else np.ones_like(mr)
+
+
 def permute(arr_csr: np.ndarray, tile_ptr: np.ndarray, sigma: int, omega: int, kind: str) -> np.ndarray:
     """CSR order -> tile order."""
     T = len(tile_ptr) - 1
@@ -40,7 +46,7 @@ def permute(arr_csr: np.ndarray, tile_ptr: np.ndarray, sigma: int, omega: int, k
     out = np.array(arr_csr, copy=True)
     if T == 0:
         return out
-    mr = multirow_tiles(tile_ptr)
+    mr = _reordered(tile_ptr, kind)
     body = out[: T * ts].reshape(T, ts)
     src = np.asarray(arr_csr)[: T * ts].reshape(T, ts)[mr]
     dst = np.empty_like(src)
@@ -56,7 +62,7 @@ def unpermute(arr_tiled: np.ndarray, tile_ptr: np.ndarray, sigma: int, omega: in
     out = np.array(arr_tiled, copy=True)
     if T == 0:
         return out
-    mr = multirow_tiles(tile_ptr)
+    mr = _reordered(tile_ptr, kind)
     body = out[: T * ts].reshape(T, ts)
     src = np.asarray(arr_tiled)[: T * ts].reshape(T, ts)[mr]
     body[mr] = src[:, positions(sigma, omega, kind)]

@@ -115,7 +115,8 @@ def test_stencil27_128_cg(native, precision):
     A = csr5.from_csr(m)
     x, res = cg(A, b, tol=1e-10, precision=precision)
     assert res.converged and res.rel_residual <= 1e-10 * 1.01
-    # the reference converges in 251 iterations on this system (single-process CG, oracle rule)
     if precision == "fp64":
-        assert abs(res.iterations - 251) <= 3
+        xo, ito, _ = _oracle_cg(m, b, 1e-10)  # the reference's CG loop on the same system
+        assert abs(res.iterations - ito) <= 2
+        assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-9
     assert np.linalg.norm(x - xs) / np.linalg.norm(xs) < 1e-6

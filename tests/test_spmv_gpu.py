@@ -127,7 +127,7 @@ def test_f32_spmv(native, torch_cuda):
     xd = torch_cuda.tensor(x, device="cuda", dtype=torch_cuda.float32)
     yd = torch_cuda.full((5000,), float("nan"), device="cuda", dtype=torch_cuda.float32)
     A.spmv(xd, yd)
-    torch_cuda.synchronize()
+    torch_cuda.cuda.synchronize()
     x32 = x.astype(np.float32).astype(np.float64)
     y_ref, ax = _refs(m, x32)
     # values rounded to f32 too: relative error per term <= 2^-24 (values) + accumulation in f32
