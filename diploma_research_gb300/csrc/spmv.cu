@@ -32,6 +32,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "common.cuh"
 #include "internal.hpp"
@@ -595,3 +596,82 @@ int check_status(dimgpu_calibrator* cal, cudaStream_t stream) {
 }
 
 }  // namespace dimgpu
+
+// ------------------------------------------------------------------------------------------------
+// SpMV without any allocation by the caller or the library.
+//
+// dimgpu_csr5_spmv needs a calibrator (scratch for the per-warp row fragments, the fused-dot
+// partials, the completion ticket and the status word), and dimgpu_calibrator_create obtains it
+// with cudaMalloc.  Some callers cannot do that: a plugin running inside a host application that
+// reserved all device memory up front, a real-time loop where cudaMalloc's implicit device
+// synchronisation would break the latency budget, or code that must not grow its memory footprint
+// after start-up.  For them the scratch of this entry point is a fixed array compiled into the
+// library: every GPU that loads the library holds it until the process exits.
+// ------------------------------------------------------------------------------------------------
+namespace dimgpu {
+namespace {
+
+constexpr uint32_t kStaticSlots = 4096;  // warp slots: enough for 256 SMs x 16 warps
+constexpr size_t kStaticValBytes = 8 * kStaticSlots;
+constexpr size_t kStaticDotBytes = 8 * (kStaticSlots + 32);
+constexpr size_t kStaticRowBytes = 4 * kStaticSlots;
+constexpr size_t kStaticWordBytes = 256;  // completion ticket + status word, own 256-byte block
+constexpr size_t kStaticScratchBytes = kStaticValBytes + kStaticDotBytes + kStaticRowBytes + kStaticWordBytes;
+
+// 82,432 bytes of device memory, shared by every call of dimgpu_csr5_spmv_static_scratch on a device.
+static __device__ __align__(256) unsigned char g_spmv_static_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mu;
+unsigned char* g_static_addr[kMaxDevices] = {};
+
+// Device address of the static scratch on `device` (which must be current).  Host code cannot use
+// the symbol itself: on the host, g_spmv_static_scratch is only a stand-in, not a device address.
+int static_scratch_on(int device, unsigned char** out) {
+    if (device < 0 || device >= kMaxDevices)
+        return fail(DIMGPU_ERR_UNSUPPORTED, "device ordinal %d is beyond %d", device, kMaxDevices);
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_addr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_spmv_static_scratch);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaGetSymbolAddress(static SpMV scratch)");
+        g_static_addr[device] = static_cast<unsigned char*>(p);
+    }
+    *out = g_static_addr[device];
+    return DIMGPU_OK;
+}
+
+}  // namespace
+}  // namespace dimgpu
+
+extern "C" int dimgpu_csr5_spmv_static_scratch(const dimgpu_csr5* m, const double* x, double* y, void* stream) {
+    using namespace dimgpu;
+    if (!m || (!x && m->cols) || (!y && m->rows))
+        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "NULL argument");
+    int device = -1;
+    DG_CUDA(cudaGetDevice(&device));
+    if (device != m->device)
+        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "the matrix lives on device %d, the current device is %d",
+                    m->device, device);
+    if (m->plan.nwarps > kStaticSlots)
+        return fail(DIMGPU_ERR_INVALID_ARGUMENT,
+                    "this matrix's SpMV uses %u warp slots; the static scratch holds at most %u "
+                    "(use dimgpu_csr5_spmv with a calibrator)",
+                    m->plan.nwarps, kStaticSlots);
+    unsigned char* base = nullptr;
+    DG_CHECK(static_scratch_on(device, &base));
+    dimgpu_calibrator cal;
+    cal.device = device;
+    cal.nslots = kStaticSlots;
+    cal.cal_val = reinterpret_cast<double*>(base);
+    cal.dot_part = reinterpret_cast<double*>(base + kStaticValBytes);
+    cal.cal_row = reinterpret_cast<uint32_t*>(base + kStaticValBytes + kStaticDotBytes);
+    cal.counter = reinterpret_cast<uint32_t*>(base + kStaticValBytes + kStaticDotBytes + kStaticRowBytes);
+    cal.status = cal.counter + 1;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // The array keeps whatever the previous call left; the completion ticket and the status word must
+    // start at zero.  (The slots themselves are written by every warp before they are read.)
+    DG_CUDA(cudaMemsetAsync(cal.counter, 0, 2 * sizeof(uint32_t), s));
+    return launch_spmv_f64(m, x, y, &cal, spmv_epilogue{}, s);
+}

@@ -111,6 +111,21 @@ DIMGPU_API int dimgpu_csr5_spmv_host(const dimgpu_csr5* m, const double* x_host,
  * The first call builds an f32 copy of the values inside the handle. */
 DIMGPU_API int dimgpu_csr5_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calibrator* cal, void* stream);
 
+/* y := A x like dimgpu_csr5_spmv, but neither this call nor the library allocates anything: the
+ * scratch (per-warp row fragments, completion ticket, status word) is a fixed array of 82,432 bytes
+ * compiled into the library, present on every GPU that loads it until the process exits.  It has no
+ * counterpart in the reference; it exists for callers that cannot allocate device memory when they
+ * multiply (a plugin whose host reserved all device memory, a latency-bound loop that cannot afford
+ * cudaMalloc's implicit synchronisation, code whose footprint must not grow after start-up).
+ *   - Limit: matrices whose SpMV launch uses more than 4096 warp slots (more than 256 SMs x 16
+ *     warps) are rejected with DIMGPU_ERR_INVALID_ARGUMENT.
+ *   - The first call on a device looks up the array's device address (cudaGetSymbolAddress) with
+ *     that device current; make that first call before any stream capture.
+ *   - Every call on a device shares the one array: calls that overlap on the GPU (different streams,
+ *     or concurrent graph branches) race and give wrong results.  Calls in one stream are safe.
+ *   - x, y: device memory of the matrix's device (the current device).  The call is asynchronous. */
+DIMGPU_API int dimgpu_csr5_spmv_static_scratch(const dimgpu_csr5* m, const double* x, double* y, void* stream);
+
 /* ---- vectors (include/dim/vec.h:29-84), device memory ----------------------------------------- */
 
 DIMGPU_API int dimgpu_vec_axpy(uint64_t n, double alpha, const double* x, double* y, void* stream); /* y += a x */
