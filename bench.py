@@ -60,7 +60,7 @@ def _profile_traffic():
 
 
 class ClockSampler:
-    """Samples nvidia-smi clocks and throttle reasons every 200 ms while alive."""
+    """Samples nvidia-smi clocks and throttle reasons every 100 ms while alive."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -74,7 +74,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=subprocess.PIPE,
                                          stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -207,8 +207,8 @@ def run_gpu(args):
     stream = torch.cuda.current_stream()
     bd = torch.tensor(b, device="cuda", dtype=torch.float64)
     xd = torch.zeros(n, device="cuda", dtype=torch.float64)
-    s64 = CGSolver(A, tol=TOL, precision="fp64", stream=stream)
-    smx = CGSolver(A, tol=TOL, precision="mixed", stream=stream)
+    s64 = CGSolver(A, tol=TOL, precision="fp64", stream=stream, use_graph=not args.no_graph)
+    smx = CGSolver(A, tol=TOL, precision="mixed", stream=stream, use_graph=not args.no_graph)
 
     def solve(solver):
         xd.zero_()
@@ -221,14 +221,14 @@ def run_gpu(args):
     if ws > 1:
         torch.distributed.barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        ev0.record(stream)
-        iters64 = []
-        for _ in range(args.steps):
-            r = solve(s64)
-            iters64.append(r.iterations)
-        ev1.record(stream)
-        torch.cuda.synchronize()
+    clk = ClockSampler(local).__enter__()  # sampled across every timed region below
+    ev0.record(stream)
+    iters64 = []
+    for _ in range(args.steps):
+        r = solve(s64)
+        iters64.append(r.iterations)
+    ev1.record(stream)
+    torch.cuda.synchronize()
     sec64 = ev0.elapsed_time(ev1) * 1e-3 / args.steps
     sec64 = _barrier_max(sec64, ws)
     err64 = float(np.linalg.norm(xd.cpu().numpy() - xs) / np.linalg.norm(xs))
@@ -264,6 +264,36 @@ def run_gpu(args):
     spmv_gbs = spmv_bytes / spmv_s / 1e9
     peak, peak_kind = _peaks()
 
+    # the CG variants of the kernel, alone: y = A x with x.y fused (f64), and the f32 product
+    from diploma_research_gb300 import _native as N
+
+    dot_d = torch.zeros(1, device="cuda", dtype=torch.float64)
+    Lb = N.lib()
+
+    def spmv_dot():
+        N.check(Lb.dimgpu_csr5_spmv_dot(A._h, x1.data_ptr(), y1.data_ptr(), dot_d.data_ptr(), cal._h,
+                                        stream.cuda_stream))
+
+    x32 = x1.float()
+    y32 = torch.empty(n, device="cuda", dtype=torch.float32)
+
+    def spmv32():
+        A.spmv(x32, y32, cal, stream=stream)
+
+    def _time(fn, reps=50):
+        for _ in range(5):
+            fn()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(reps):
+            fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) * 1e-3 / reps
+
+    spmv_dot_s = _time(spmv_dot)
+    spmv32_s = _time(spmv32)
+
     # ---- e2e: the same FP64 solve through the C ABI with pinned host buffers ----
     bh = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
     bh[:] = b
@@ -284,6 +314,7 @@ def run_gpu(args):
         N.check(L.dimgpu_cg_solve_host(s64._h, bh.ctypes.data, xh.ctypes.data, ctypes.byref(st)))
         e2e_t.append(time.perf_counter() - t)
     e2e_s = _barrier_max(statistics.mean(e2e_t), ws)
+    clk.__exit__(None, None, None)
 
     # ---- CPU baseline: the reference's CPU CG (C restatement), full solve, rank 0 only ----
     cpu = None
@@ -315,7 +346,8 @@ def run_gpu(args):
                       "reliable_updates": resm.reliable_updates, "rel_residual": resm.rel_residual,
                       "rel_error_vs_xstar": errm, "speedup_vs_fp64": sec64 / secm, "dtype": "f32 inner / f64"},
             "spmv": {"seconds": spmv_s, "gbps": spmv_gbs, "bytes_per_launch": spmv_bytes,
-                     "fp64_tflops": 2 * nnz / spmv_s / 1e12},
+                     "fp64_tflops": 2 * nnz / spmv_s / 1e12, "dot_fused_seconds": spmv_dot_s,
+                     "f32_seconds": spmv32_s, "f32_gbps": (8 * nnz + 8 * n) / spmv32_s / 1e9},
             "roofline": {"bound": "hbm", "achieved": spmv_gbs, "peak": peak, "unit": "GB/s",
                          "frac": spmv_gbs / peak, "traffic": _profile_traffic(), "kernel": "k_spmv<double,16>",
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
@@ -346,8 +378,9 @@ def run_spmv_only(args):
     n, nnz = m.dimensions.rows, m.nnz
     A = csr5.from_csr(m)
     stream = torch.cuda.current_stream()
-    x = torch.tensor(np.random.default_rng(5).uniform(-1, 1, n), device="cuda", dtype=torch.float64)
-    y = torch.empty(n, device="cuda", dtype=torch.float64)
+    dt = torch.float32 if args.f32 else torch.float64
+    x = torch.tensor(np.random.default_rng(5).uniform(-1, 1, n), device="cuda", dtype=dt)
+    y = torch.empty(n, device="cuda", dtype=dt)
     cal = A.create_calibrator()
     for _ in range(5):
         A.spmv(x, y, cal, stream=stream)
@@ -359,7 +392,8 @@ def run_spmv_only(args):
     ev1.record(stream)
     torch.cuda.synchronize()
     s = ev0.elapsed_time(ev1) * 1e-3 / args.steps
-    print(json.dumps({"spmv_seconds": s, "gbps": (12 * nnz + 16 * n) / s / 1e9, "nnz": nnz, "n": n}))
+    nbytes = (8 * nnz + 8 * n) if args.f32 else (12 * nnz + 16 * n)
+    print(json.dumps({"spmv_seconds": s, "gbps": nbytes / s / 1e9, "nnz": nnz, "n": n, "f32": bool(args.f32)}))
     return 0
 
 
@@ -371,6 +405,9 @@ def main():
     ap.add_argument("--impl", default="dimgpu", choices=["dimgpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--spmv-only", action="store_true", help="few SpMV launches only (for profiler captures)")
+    ap.add_argument("--f32", action="store_true", help="with --spmv-only: the f32 product")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="host-driven CG loop instead of the CUDA graph (profilers list every kernel)")
     args = ap.parse_args()
     if args.spmv_only:
         return run_spmv_only(args)

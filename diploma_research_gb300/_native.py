@@ -92,6 +92,7 @@ _SIGNATURES = {
     "dimgpu_calibrator_destroy": [_vp],
     "dimgpu_csr5_spmv": [_vp, _vp, _vp, _vp, _vp],
     "dimgpu_csr5_spmv_host": [_vp, _vp, _vp],
+    "dimgpu_csr5_spmv_dot": [_vp, _vp, _vp, _vp, _vp, _vp],
     "dimgpu_csr5_spmv_f32": [_vp, _vp, _vp, _vp, _vp],
     "dimgpu_vec_axpy": [_u64, _f64, _vp, _vp, _vp],
     "dimgpu_vec_aypx": [_u64, _f64, _vp, _vp, _vp],

@@ -237,7 +237,8 @@ int dimgpu_csr5_from_csr(uint32_t rows, uint32_t cols, uint64_t nnz, const uint3
         }
         if ((rc = prepare_spmv_kernels()) != DIMGPU_OK) break;
         if ((rc = convert_csr5(m, d_rp, d_ci, d_v, s)) != DIMGPU_OK) break;
-        m->plan = make_spmv_plan(m->tile_count, device_sm_count(m->device));
+        m->plan = make_spmv_plan(m->tile_count, device_sm_count(m->device), 16);
+        m->plan32 = make_spmv_plan32(m->tile_count, device_sm_count(m->device));
         m->own_cal = new dimgpu_calibrator();
         if ((rc = calibrator_init(m->own_cal, m)) != DIMGPU_OK) break;
     } while (false);
@@ -325,6 +326,17 @@ int dimgpu_csr5_spmv(const dimgpu_csr5* m, const double* x, double* y, dimgpu_ca
     if (!m || (!x && m->cols) || (!y && m->rows))
         return fail(DIMGPU_ERR_INVALID_ARGUMENT, "NULL argument");
     return launch_spmv_f64(m, x, y, cal ? cal : m->own_cal, spmv_epilogue{}, static_cast<cudaStream_t>(stream));
+}
+
+int dimgpu_csr5_spmv_dot(const dimgpu_csr5* m, const double* x, double* y, double* dot, dimgpu_calibrator* cal,
+                         void* stream) {
+    if (!m || (!x && m->cols) || (!y && m->rows) || !dot)
+        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (m->rows != m->cols)
+        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "x.(A x) needs a square matrix (%u x %u)", m->rows, m->cols);
+    spmv_epilogue ep;
+    ep.dot_out = dot;
+    return launch_spmv_f64(m, x, y, cal ? cal : m->own_cal, ep, static_cast<cudaStream_t>(stream));
 }
 
 int dimgpu_csr5_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calibrator* cal, void* stream) {

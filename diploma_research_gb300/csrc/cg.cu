@@ -5,18 +5,23 @@
 // sqrt(r.r) <= tol * ||b||:
 //     As = A s; alpha = rr / (s.As); x += alpha s; r -= alpha As; rr' = r.r; beta = rr'/rr; s = r + beta s
 //
-// One iteration is three kernels, all deterministic (fixed grids, fixed-order reductions):
+// FP64 iteration = three kernels, all deterministic (fixed grids, fixed-order reductions):
 //   A  SpMV As = A s fused with s.As and alpha = rr / s.As (spmv.cu's last-CTA epilogue)
 //   B  r -= alpha As and r.r; its last block decides convergence, beta and the loop condition
 //   C  x += alpha s and s = r + beta s in one pass (x is updated here, from the old s)
-// and the whole solve is one CUDA graph: init kernels, then a conditional WHILE node whose body is
-// A, B, C; B sets the loop condition from the device, so the solve runs without host round trips.
+// The whole solve is one CUDA graph: init kernels, then a conditional WHILE node whose body is the
+// iteration; kernel B sets the loop condition from the device, so the solve makes no host round trip.
 //
-// The mixed-precision solver runs the same recurrence on f32 values and f32 vectors s, As, r with
-// f64 dot products, f64 alpha/beta and an f64 iterate x, and replaces the recurrence residual by the
-// true f64 residual b - A x ("reliable update") whenever r.r has dropped by reliable_delta^2 since
-// the last replacement, and before convergence is accepted.  Convergence is only declared on a true
-// f64 residual, so the mixed solver meets the same ||b - A x|| <= tol ||b|| as the f64 solver.
+// Mixed precision runs the same recurrence on f32 values and f32 vectors s, As, r.  Products and short
+// partial sums are f32, every dot product is accumulated in f64, alpha and beta are f64, and the
+// iterate is kept as x (f64) + y (f32 correction since the last flush).  Whenever r.r has dropped by
+// reliable_delta^2 since the last replacement, before convergence is accepted and at max_it, a
+// reliable update flushes y into x and replaces r by the true f64 residual b - A x computed with the
+// f64 matrix.  Convergence is declared on a true f64 residual only.  Iteration kernels:
+//   A32 SpMV (f32) + s.As + alpha;  B32 r -= alpha As, y += alpha s, r.r, decides a reliable update;
+//   IF(reliable update) { x += y, y = 0;  Ax = A x (f64 SpMV);  r = b - Ax, r.r (f64) };
+//   S32 s = r + beta s.
+// The IF is a conditional graph node, so iterations without a reliable update launch three kernels.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -31,6 +36,7 @@ namespace dimgpu {
 namespace {
 
 constexpr int kVecThreads = 512;
+constexpr int kUnroll = 4;
 
 struct cg_state {
     double rr;       // r.r of the current residual
@@ -44,7 +50,7 @@ struct cg_state {
     double rr_true;  // last true residual r.r (f64)
     int64_t iter, max_it, ru_count;
     uint32_t stop;       // the solve has finished
-    uint32_t x_pending;  // kernel C owes x += alpha s
+    uint32_t x_pending;  // f64: kernel C owes x += alpha s
     uint32_t no_ru;      // mixed: no reliable update this iteration (guards its kernels)
     uint32_t converged;
 };
@@ -53,8 +59,9 @@ struct vec_ctx {
     cg_state* st;
     double* part;       // [grid * 2] block partials
     uint32_t* counter;  // completion ticket
-    cudaGraphConditionalHandle cond;
-    int has_cond;
+    cudaGraphConditionalHandle loop;
+    cudaGraphConditionalHandle ru;
+    int has_loop, has_ru;
 };
 
 // Reduces (a, b) over the grid.  Returns true in exactly one thread (thread 0 of the last block to
@@ -112,15 +119,36 @@ __device__ bool grid_reduce2(double a, double b, const vec_ctx& c, double* ta, d
     return true;
 }
 
-__device__ __forceinline__ void set_cond(const vec_ctx& c, bool go) {
-    if (c.has_cond)
-        cudaGraphSetConditional(c.cond, go ? 1u : 0u);
+__device__ __forceinline__ void set_loop(const vec_ctx& c, bool go) {
+    if (c.has_loop)
+        cudaGraphSetConditional(c.loop, go ? 1u : 0u);
+}
+__device__ __forceinline__ void set_ru(const vec_ctx& c, bool go) {
+    if (c.has_ru)
+        cudaGraphSetConditional(c.ru, go ? 1u : 0u);
 }
 
+// Calls f(i) for every vector index i in [0, nv), kUnroll grid strides at a time so that each thread
+// keeps several independent 16-byte accesses in flight.
 template <typename F>
-__device__ __forceinline__ void grid_loop(uint64_t n, F f) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+__device__ __forceinline__ void vloop(uint64_t nv, F f) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    for (; i + (kUnroll - 1) * stride < nv; i += kUnroll * stride) {
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u)
+            f(i + u * stride);
+    }
+    for (; i < nv; i += stride)
         f(i);
+}
+
+// The scalar elements past the last full vector, visited by the first threads of block 0.
+template <typename F>
+__device__ __forceinline__ void vtail(uint64_t n, uint64_t width, F f) {
+    const uint64_t first = (n / width) * width;
+    if (blockIdx.x == 0 && first + threadIdx.x < n)
+        f(first + threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -130,14 +158,22 @@ __device__ __forceinline__ void grid_loop(uint64_t n, F f) {
 // r = b - Ax; s = r; rr = r.r; bb = b.b
 __global__ void __launch_bounds__(kVecThreads) k_init64(const double* b, const double* Ax, double* r, double* s,
                                                         uint64_t n, vec_ctx c) {
+    const uint64_t pol = policy_evict_last();
     double rr = 0, bb = 0;
-    grid_loop(n, [&](uint64_t i) {
-        const double bi = b[i];
-        const double ri = bi - Ax[i];
+    vloop(n / 2, [&](uint64_t i) {
+        const double2 bi = ld2_keep(b + 2 * i, pol), ai = ld2_keep(Ax + 2 * i, pol);
+        const double2 ri = make_double2(bi.x - ai.x, bi.y - ai.y);
+        st2_keep(r + 2 * i, ri, pol);
+        st2_keep(s + 2 * i, ri, pol);
+        rr = fma(ri.x, ri.x, fma(ri.y, ri.y, rr));
+        bb = fma(bi.x, bi.x, fma(bi.y, bi.y, bb));
+    });
+    vtail(n, 2, [&](uint64_t i) {
+        const double ri = b[i] - Ax[i];
         r[i] = ri;
         s[i] = ri;
         rr = fma(ri, ri, rr);
-        bb = fma(bi, bi, bb);
+        bb = fma(b[i], b[i], bb);
     });
     double trr, tbb;
     if (grid_reduce2(rr, bb, c, &trr, &tbb)) {
@@ -149,24 +185,35 @@ __global__ void __launch_bounds__(kVecThreads) k_init64(const double* b, const d
         st->x_pending = 0;
         st->converged = trr <= st->thresh2 ? 1u : 0u;
         st->stop = st->converged || st->max_it <= 0;
-        set_cond(c, !st->stop);
+        set_loop(c, !st->stop);
     }
 }
 
 // r -= alpha As; rr' = r.r; decide
 __global__ void __launch_bounds__(kVecThreads) k_update_r64(const double* As, double* r, uint64_t n, vec_ctx c) {
     cg_state* st = c.st;
-    if (*reinterpret_cast<volatile uint32_t*>(&st->stop)) {
+    // the state was written by earlier kernels: read it once, both words in flight together
+    const uint32_t stop = st->stop;
+    const double alpha = st->alpha;
+    if (stop) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             st->x_pending = 0;
-            set_cond(c, false);
+            set_loop(c, false);
         }
         return;
     }
-    const double alpha = st->alpha;
+    const uint64_t pol = policy_evict_last();
     double rr = 0;
-    grid_loop(n, [&](uint64_t i) {
-        const double ri = r[i] + -alpha * As[i];
+    vloop(n / 2, [&](uint64_t i) {
+        const double2 a = ld2_keep(As + 2 * i, pol);
+        double2 q = ld2_keep(r + 2 * i, pol);
+        q.x = fma(-alpha, a.x, q.x);
+        q.y = fma(-alpha, a.y, q.y);
+        st2_keep(r + 2 * i, q, pol);
+        rr = fma(q.x, q.x, fma(q.y, q.y, rr));
+    });
+    vtail(n, 2, [&](uint64_t i) {
+        const double ri = fma(-alpha, As[i], r[i]);
         r[i] = ri;
         rr = fma(ri, ri, rr);
     });
@@ -184,43 +231,68 @@ __global__ void __launch_bounds__(kVecThreads) k_update_r64(const double* As, do
             st->beta = t / st->rr;
         }
         st->rr = t;
-        set_cond(c, !st->stop);
+        set_loop(c, !st->stop);
     }
 }
 
 // x += alpha s; s = r + beta s (the latter only while the solve continues)
 __global__ void __launch_bounds__(kVecThreads) k_update_xs64(double* x, double* s, const double* r, uint64_t n,
                                                              const cg_state* st) {
-    if (!*reinterpret_cast<const volatile uint32_t*>(&st->x_pending))
-        return;
+    const uint32_t pending = st->x_pending, stop = st->stop;
     const double alpha = st->alpha, beta = st->beta;
-    const bool more = !*reinterpret_cast<const volatile uint32_t*>(&st->stop);
-    if (more)
-        grid_loop(n, [&](uint64_t i) {
-            const double si = s[i];
-            x[i] = x[i] + alpha * si;
-            s[i] = r[i] + beta * si;
+    if (!pending)
+        return;
+    const uint64_t pol = policy_evict_last();
+    const bool more = !stop;
+    if (more) {
+        vloop(n / 2, [&](uint64_t i) {
+            const double2 si = ld2_keep(s + 2 * i, pol), xi = ld2_keep(x + 2 * i, pol), ri = ld2_keep(r + 2 * i, pol);
+            st2_keep(x + 2 * i, make_double2(fma(alpha, si.x, xi.x), fma(alpha, si.y, xi.y)), pol);
+            st2_keep(s + 2 * i, make_double2(fma(beta, si.x, ri.x), fma(beta, si.y, ri.y)), pol);
         });
-    else
-        grid_loop(n, [&](uint64_t i) { x[i] = x[i] + alpha * s[i]; });
+        vtail(n, 2, [&](uint64_t i) {
+            const double si = s[i];
+            x[i] = fma(alpha, si, x[i]);
+            s[i] = fma(beta, si, r[i]);
+        });
+    } else {
+        vloop(n / 2, [&](uint64_t i) {
+            const double2 si = ld2_keep(s + 2 * i, pol), xi = ld2_keep(x + 2 * i, pol);
+            st2_keep(x + 2 * i, make_double2(fma(alpha, si.x, xi.x), fma(alpha, si.y, xi.y)), pol);
+        });
+        vtail(n, 2, [&](uint64_t i) { x[i] = fma(alpha, s[i], x[i]); });
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
-// mixed solver: f32 inner recurrence, f64 x and reliable f64 residual updates
+// mixed solver
 // ---------------------------------------------------------------------------------------------
 
-// r64 = b - Ax; r32 = s32 = r64; rr = r64.r64; bb = b.b
+__device__ __forceinline__ float sq4(float4 v) { return fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, v.w * v.w))); }
+
+// r64 = b - Ax; r32 = s32 = r64; y32 = 0; rr = r64.r64; bb = b.b
 __global__ void __launch_bounds__(kVecThreads) k_init_mixed(const double* b, const double* Ax, float* r32, float* s32,
-                                                            uint64_t n, vec_ctx c) {
+                                                            float* y32, uint64_t n, vec_ctx c) {
+    const uint64_t pol = policy_evict_last();
     double rr = 0, bb = 0;
-    grid_loop(n, [&](uint64_t i) {
-        const double bi = b[i];
-        const double ri = bi - Ax[i];
-        const float rf = (float)ri;
-        r32[i] = rf;
-        s32[i] = rf;
+    vloop(n / 4, [&](uint64_t i) {
+        const double2 b0 = ld2_keep(b + 4 * i, pol), b1 = ld2_keep(b + 4 * i + 2, pol);
+        const double2 a0 = ld2_keep(Ax + 4 * i, pol), a1 = ld2_keep(Ax + 4 * i + 2, pol);
+        const double r0 = b0.x - a0.x, r1 = b0.y - a0.y, r2 = b1.x - a1.x, r3 = b1.y - a1.y;
+        const float4 rf = make_float4((float)r0, (float)r1, (float)r2, (float)r3);
+        st4_keep(r32 + 4 * i, rf, pol);
+        st4_keep(s32 + 4 * i, rf, pol);
+        st4_keep(y32 + 4 * i, make_float4(0.f, 0.f, 0.f, 0.f), pol);
+        rr = fma(r0, r0, fma(r1, r1, fma(r2, r2, fma(r3, r3, rr))));
+        bb = fma(b0.x, b0.x, fma(b0.y, b0.y, fma(b1.x, b1.x, fma(b1.y, b1.y, bb))));
+    });
+    vtail(n, 4, [&](uint64_t i) {
+        const double ri = b[i] - Ax[i];
+        r32[i] = (float)ri;
+        s32[i] = (float)ri;
+        y32[i] = 0.f;
         rr = fma(ri, ri, rr);
-        bb = fma(bi, bi, bb);
+        bb = fma(b[i], b[i], bb);
     });
     double trr, tbb;
     if (grid_reduce2(rr, bb, c, &trr, &tbb)) {
@@ -236,33 +308,46 @@ __global__ void __launch_bounds__(kVecThreads) k_init_mixed(const double* b, con
         st->no_ru = 1;
         st->converged = trr <= st->thresh2 ? 1u : 0u;
         st->stop = st->converged || st->max_it <= 0;
-        set_cond(c, !st->stop);
+        set_loop(c, !st->stop);
     }
 }
 
-// r32 -= alpha As32; rr' = r32.r32 (f64 sum); decide whether a reliable update is due
-__global__ void __launch_bounds__(kVecThreads) k_update_r_mixed(const float* As, float* r, uint64_t n, vec_ctx c) {
+// r32 -= alpha As32; y32 += alpha s32; rr' = r32.r32 (f32 partials of 4, summed in f64); decide whether a
+// reliable update is due
+__global__ void __launch_bounds__(kVecThreads) k_update_r_mixed(const float* As, float* r, const float* s, float* y,
+                                                                uint64_t n, vec_ctx c) {
     cg_state* st = c.st;
-    if (*reinterpret_cast<volatile uint32_t*>(&st->stop)) {
+    const uint32_t stop = st->stop;
+    const float af = (float)st->alpha;
+    if (stop) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
-            st->x_pending = 0;
             st->no_ru = 1;
-            set_cond(c, false);
+            set_ru(c, false);
+            set_loop(c, false);
         }
         return;
     }
-    const double alpha = st->alpha;
+    const uint64_t pol = policy_evict_last();
     double rr = 0;
-    grid_loop(n, [&](uint64_t i) {
-        const float ri = (float)((double)r[i] - alpha * (double)As[i]);
-        r[i] = ri;
-        rr = fma((double)ri, (double)ri, rr);
+    vloop(n / 4, [&](uint64_t i) {
+        const float4 a = ld4_keep(As + 4 * i, pol), si = ld4_keep(s + 4 * i, pol);
+        float4 q = ld4_keep(r + 4 * i, pol), yi = ld4_keep(y + 4 * i, pol);
+        q = make_float4(fmaf(-af, a.x, q.x), fmaf(-af, a.y, q.y), fmaf(-af, a.z, q.z), fmaf(-af, a.w, q.w));
+        yi = make_float4(fmaf(af, si.x, yi.x), fmaf(af, si.y, yi.y), fmaf(af, si.z, yi.z), fmaf(af, si.w, yi.w));
+        st4_keep(r + 4 * i, q, pol);
+        st4_keep(y + 4 * i, yi, pol);
+        rr += (double)sq4(q);
+    });
+    vtail(n, 4, [&](uint64_t i) {
+        const float q = fmaf(-af, As[i], r[i]);
+        r[i] = q;
+        y[i] = fmaf(af, s[i], y[i]);
+        rr += (double)(q * q);
     });
     double t, unused;
     if (grid_reduce2(rr, 0.0, c, &t, &unused)) {
         st->rr_new = t;
         st->iter += 1;
-        st->x_pending = 1;
         const bool ru = t <= st->thresh2 || t < st->delta2 * st->maxrr || st->iter >= st->max_it || !isfinite(t);
         st->no_ru = ru ? 0u : 1u;
         if (!ru) {
@@ -270,27 +355,46 @@ __global__ void __launch_bounds__(kVecThreads) k_update_r_mixed(const float* As,
             st->rr = t;
             st->maxrr = fmax(st->maxrr, t);
         }
-        set_cond(c, true);
+        set_ru(c, ru);
+        set_loop(c, true);
     }
 }
 
-// reliable update, part 1: x += alpha s (the step of this iteration, before b - A x is formed)
-__global__ void __launch_bounds__(kVecThreads) k_ru_x_mixed(double* x, const float* s, uint64_t n,
-                                                            const cg_state* st) {
-    if (*reinterpret_cast<const volatile uint32_t*>(&st->no_ru))
+// x += y; y = 0 (at reliable updates and at the end of the solve)
+__global__ void __launch_bounds__(kVecThreads) k_flush_mixed(double* x, float* y, uint64_t n, const cg_state* st,
+                                                             int guarded) {
+    if (guarded && *reinterpret_cast<const volatile uint32_t*>(&st->no_ru))
         return;
-    const double alpha = st->alpha;
-    grid_loop(n, [&](uint64_t i) { x[i] = x[i] + alpha * (double)s[i]; });
+    const uint64_t pol = policy_evict_last();
+    vloop(n / 4, [&](uint64_t i) {
+        const float4 yi = ld4_keep(y + 4 * i, pol);
+        const double2 x0 = ld2_keep(x + 4 * i, pol), x1 = ld2_keep(x + 4 * i + 2, pol);
+        st2_keep(x + 4 * i, make_double2(x0.x + (double)yi.x, x0.y + (double)yi.y), pol);
+        st2_keep(x + 4 * i + 2, make_double2(x1.x + (double)yi.z, x1.y + (double)yi.w), pol);
+        st4_keep(y + 4 * i, make_float4(0.f, 0.f, 0.f, 0.f), pol);
+    });
+    vtail(n, 4, [&](uint64_t i) {
+        x[i] += (double)y[i];
+        y[i] = 0.f;
+    });
 }
 
-// reliable update, part 2 (after Ax = A x in f64): r64 = b - Ax; r32 = r64; decide convergence
+// reliable update, after Ax = A x in f64: r32 = b - Ax; decide convergence on the true residual
 __global__ void __launch_bounds__(kVecThreads) k_ru_r_mixed(const double* b, const double* Ax, float* r32, uint64_t n,
                                                             vec_ctx c) {
     cg_state* st = c.st;
     if (*reinterpret_cast<volatile uint32_t*>(&st->no_ru))
         return;
+    const uint64_t pol = policy_evict_last();
     double rr = 0;
-    grid_loop(n, [&](uint64_t i) {
+    vloop(n / 4, [&](uint64_t i) {
+        const double2 b0 = ld2_keep(b + 4 * i, pol), b1 = ld2_keep(b + 4 * i + 2, pol);
+        const double2 a0 = ld2_keep(Ax + 4 * i, pol), a1 = ld2_keep(Ax + 4 * i + 2, pol);
+        const double r0 = b0.x - a0.x, r1 = b0.y - a0.y, r2 = b1.x - a1.x, r3 = b1.y - a1.y;
+        st4_keep(r32 + 4 * i, make_float4((float)r0, (float)r1, (float)r2, (float)r3), pol);
+        rr = fma(r0, r0, fma(r1, r1, fma(r2, r2, fma(r3, r3, rr))));
+    });
+    vtail(n, 4, [&](uint64_t i) {
         const double ri = b[i] - Ax[i];
         r32[i] = (float)ri;
         rr = fma(ri, ri, rr);
@@ -299,7 +403,6 @@ __global__ void __launch_bounds__(kVecThreads) k_ru_r_mixed(const double* b, con
     if (grid_reduce2(rr, 0.0, c, &t, &unused)) {
         st->ru_count += 1;
         st->rr_true = t;
-        st->x_pending = 0;  // x already holds this iteration's step
         if (t <= st->thresh2) {
             st->converged = 1;
             st->stop = 1;
@@ -310,36 +413,36 @@ __global__ void __launch_bounds__(kVecThreads) k_ru_r_mixed(const double* b, con
             st->rr = t;
             st->maxrr = t;
         }
-        set_cond(c, !st->stop);
+        set_loop(c, !st->stop);
     }
 }
 
-// x += alpha s (unless the reliable update did it); s32 = r32 + beta s32 while the solve continues
-__global__ void __launch_bounds__(kVecThreads) k_update_xs_mixed(double* x, float* s, const float* r, uint64_t n,
-                                                                 const cg_state* st) {
-    const bool xp = *reinterpret_cast<const volatile uint32_t*>(&st->x_pending) != 0;
-    const bool more = !*reinterpret_cast<const volatile uint32_t*>(&st->stop);
-    if (!xp && !more)
-        return;
-    const double alpha = st->alpha;
+// s32 = r32 + beta s32 while the solve continues
+__global__ void __launch_bounds__(kVecThreads) k_update_s_mixed(float* s, const float* r, uint64_t n,
+                                                                const cg_state* st) {
+    const uint32_t stop = st->stop;
     const float beta = (float)st->beta;
-    grid_loop(n, [&](uint64_t i) {
-        const float si = s[i];
-        if (xp)
-            x[i] = x[i] + alpha * (double)si;
-        if (more)
-            s[i] = fmaf(beta, si, r[i]);
+    if (stop)
+        return;
+    const uint64_t pol = policy_evict_last();
+    vloop(n / 4, [&](uint64_t i) {
+        const float4 si = ld4_keep(s + 4 * i, pol), ri = ld4_keep(r + 4 * i, pol);
+        st4_keep(s + 4 * i,
+                 make_float4(fmaf(beta, si.x, ri.x), fmaf(beta, si.y, ri.y), fmaf(beta, si.z, ri.z),
+                             fmaf(beta, si.w, ri.w)),
+                 pol);
     });
+    vtail(n, 4, [&](uint64_t i) { s[i] = fmaf(beta, s[i], r[i]); });
 }
 
 __global__ void k_residual_norms(const double* b, const double* Ax, uint64_t n, double* out2) {
     // out2[0] += (b-Ax).(b-Ax) partial, out2[1] += b.b partial (atomics: diagnostics only)
     double rr = 0, bb = 0;
-    grid_loop(n, [&](uint64_t i) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const double ri = b[i] - Ax[i];
         rr = fma(ri, ri, rr);
         bb = fma(b[i], b[i], bb);
-    });
+    }
     rr = warp_sum(rr);
     bb = warp_sum(bb);
     if ((threadIdx.x & 31u) == 0) {
@@ -361,12 +464,12 @@ struct dimgpu_cg_solver {
     // f64 vectors
     double *b = nullptr, *x = nullptr, *r = nullptr, *s = nullptr, *As = nullptr, *Ax = nullptr;
     // f32 vectors (mixed)
-    float *r32 = nullptr, *s32 = nullptr, *As32 = nullptr;
+    float *r32 = nullptr, *s32 = nullptr, *As32 = nullptr, *y32 = nullptr;
     cg_state* st = nullptr;
     double* part = nullptr;
     uint32_t* counter = nullptr;
     double* norms = nullptr;
-    dimgpu_calibrator cal{};   // SpMV scratch of this solver (f32 and f64 products take turns)
+    dimgpu_calibrator cal{};  // SpMV scratch of this solver (f32 and f64 products take turns)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -387,52 +490,62 @@ void solver_free(dimgpu_cg_solver* s) {
         cudaEventDestroy(s->ev1);
     calibrator_release(&s->cal);
     for (void* p : {(void*)s->b, (void*)s->x, (void*)s->r, (void*)s->s, (void*)s->As, (void*)s->Ax, (void*)s->r32,
-                    (void*)s->s32, (void*)s->As32, (void*)s->st, (void*)s->part, (void*)s->counter, (void*)s->norms})
+                    (void*)s->s32, (void*)s->As32, (void*)s->y32, (void*)s->st, (void*)s->part, (void*)s->counter,
+                    (void*)s->norms})
         dev_free(p);
     delete s;
 }
 
-vec_ctx make_ctx(dimgpu_cg_solver* s, cudaGraphConditionalHandle h, int has) {
-    vec_ctx c;
+vec_ctx make_ctx(dimgpu_cg_solver* s) {
+    vec_ctx c{};
     c.st = s->st;
     c.part = s->part;
     c.counter = s->counter;
-    c.cond = h;
-    c.has_cond = has;
     return c;
 }
 
+bool mixed(const dimgpu_cg_solver* s) { return s->params.precision == DIMGPU_CG_MIXED; }
+
 // Enqueues the init kernels (needs s->x and s->b filled).
-int enqueue_init(dimgpu_cg_solver* s, cudaGraphConditionalHandle h, int has, cudaStream_t st) {
-    vec_ctx c = make_ctx(s, h, has);
+int enqueue_init(dimgpu_cg_solver* s, const vec_ctx& c, cudaStream_t st) {
     DG_CHECK(launch_spmv_f64(s->m, s->x, s->Ax, &s->cal, spmv_epilogue{}, st));
-    if (s->params.precision == DIMGPU_CG_MIXED)
-        k_init_mixed<<<s->grid, kVecThreads, 0, st>>>(s->b, s->Ax, s->r32, s->s32, s->n, c);
+    if (mixed(s))
+        k_init_mixed<<<s->grid, kVecThreads, 0, st>>>(s->b, s->Ax, s->r32, s->s32, s->y32, s->n, c);
     else
         k_init64<<<s->grid, kVecThreads, 0, st>>>(s->b, s->Ax, s->r, s->s, s->n, c);
     DG_CUDA(cudaGetLastError());
     return DIMGPU_OK;
 }
 
-// Enqueues one iteration.
-int enqueue_iteration(dimgpu_cg_solver* s, cudaGraphConditionalHandle h, int has, cudaStream_t st) {
-    vec_ctx c = make_ctx(s, h, has);
+spmv_epilogue cg_epilogue(dimgpu_cg_solver* s) {
     spmv_epilogue ep;
     ep.dot_out = &s->st->dot;
     ep.rr = &s->st->rr;
     ep.alpha_out = &s->st->alpha;
     ep.halt = &s->st->stop;
-    if (s->params.precision == DIMGPU_CG_MIXED) {
-        DG_CHECK(launch_spmv_f32(s->m, s->s32, s->As32, &s->cal, ep, st));
-        k_update_r_mixed<<<s->grid, kVecThreads, 0, st>>>(s->As32, s->r32, s->n, c);
-        k_ru_x_mixed<<<s->grid, kVecThreads, 0, st>>>(s->x, s->s32, s->n, s->st);
-        spmv_epilogue ru;
-        ru.halt = &s->st->no_ru;
-        DG_CHECK(launch_spmv_f64(s->m, s->x, s->Ax, &s->cal, ru, st));
-        k_ru_r_mixed<<<s->grid, kVecThreads, 0, st>>>(s->b, s->Ax, s->r32, s->n, c);
-        k_update_xs_mixed<<<s->grid, kVecThreads, 0, st>>>(s->x, s->s32, s->r32, s->n, s->st);
+    return ep;
+}
+
+// The reliable-update kernels of the mixed solver (each guarded by st->no_ru).
+int enqueue_reliable_update(dimgpu_cg_solver* s, const vec_ctx& c, cudaStream_t st) {
+    k_flush_mixed<<<s->grid, kVecThreads, 0, st>>>(s->x, s->y32, s->n, s->st, 1);
+    spmv_epilogue ru;
+    ru.halt = &s->st->no_ru;
+    DG_CHECK(launch_spmv_f64(s->m, s->x, s->Ax, &s->cal, ru, st));
+    k_ru_r_mixed<<<s->grid, kVecThreads, 0, st>>>(s->b, s->Ax, s->r32, s->n, c);
+    DG_CUDA(cudaGetLastError());
+    return DIMGPU_OK;
+}
+
+// One whole iteration as a plain stream of kernels (host-driven loop).
+int enqueue_iteration(dimgpu_cg_solver* s, const vec_ctx& c, cudaStream_t st) {
+    if (mixed(s)) {
+        DG_CHECK(launch_spmv_f32(s->m, s->s32, s->As32, &s->cal, cg_epilogue(s), st));
+        k_update_r_mixed<<<s->grid, kVecThreads, 0, st>>>(s->As32, s->r32, s->s32, s->y32, s->n, c);
+        DG_CHECK(enqueue_reliable_update(s, c, st));
+        k_update_s_mixed<<<s->grid, kVecThreads, 0, st>>>(s->s32, s->r32, s->n, s->st);
     } else {
-        DG_CHECK(launch_spmv_f64(s->m, s->s, s->As, &s->cal, ep, st));
+        DG_CHECK(launch_spmv_f64(s->m, s->s, s->As, &s->cal, cg_epilogue(s), st));
         k_update_r64<<<s->grid, kVecThreads, 0, st>>>(s->As, s->r, s->n, c);
         k_update_xs64<<<s->grid, kVecThreads, 0, st>>>(s->x, s->s, s->r, s->n, s->st);
     }
@@ -440,78 +553,105 @@ int enqueue_iteration(dimgpu_cg_solver* s, cudaGraphConditionalHandle h, int has
     return DIMGPU_OK;
 }
 
-int build_graph(dimgpu_cg_solver* s, cudaStream_t stream) {
+// Captures `body` into `graph` after `deps`; returns the capture's leaf nodes in *leaves.
+template <typename F>
+int capture_into(cudaStream_t cap, cudaGraph_t graph, const std::vector<cudaGraphNode_t>& deps,
+                 std::vector<cudaGraphNode_t>* leaves, F body) {
+    cudaError_t e = cudaStreamBeginCaptureToGraph(cap, graph, deps.empty() ? nullptr : deps.data(), nullptr,
+                                                  deps.size(), cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "begin capture");
+    int rc = body();
+    if (rc == DIMGPU_OK && leaves) {
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t* d = nullptr;
+        size_t nd = 0;
+        e = cudaStreamGetCaptureInfo(cap, &cs, nullptr, nullptr, &d, nullptr, &nd);
+        if (e != cudaSuccess)
+            rc = cuda_fail(e, "capture info");
+        else
+            leaves->assign(d, d + nd);
+    }
+    cudaGraph_t out;
+    e = cudaStreamEndCapture(cap, &out);
+    if (rc == DIMGPU_OK && e != cudaSuccess)
+        rc = cuda_fail(e, "end capture");
+    return rc;
+}
+
+int add_conditional(cudaGraph_t graph, const std::vector<cudaGraphNode_t>& deps, cudaGraphConditionalHandle h,
+                    cudaGraphConditionalNodeType type, cudaGraphNode_t* node, cudaGraph_t* body) {
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = type;
+    cp.conditional.size = 1;
+    DG_CUDA(cudaGraphAddNode(node, graph, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(), &cp));
+    *body = cp.conditional.phGraph_out[0];
+    return DIMGPU_OK;
+}
+
+// Graph: init kernels -> WHILE(loop) { iteration }.  The mixed iteration is
+// A32 -> B32 -> IF(ru) { flush, f64 SpMV, residual } -> S32.
+int build_graph(dimgpu_cg_solver* s) {
     cudaGraph_t g = nullptr;
     DG_CUDA(cudaGraphCreate(&g, 0));
-    cudaGraphConditionalHandle h;
-    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0, 0);
-    if (e != cudaSuccess) {
-        cudaGraphDestroy(g);
-        return cuda_fail(e, "cudaGraphConditionalHandleCreate");
-    }
-    int rc = DIMGPU_OK;
     cudaStream_t cap = nullptr;
-    e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         cudaGraphDestroy(g);
         return cuda_fail(e, "cudaStreamCreate");
     }
+    int rc = DIMGPU_OK;
     do {
-        // init part
-        e = cudaStreamBeginCaptureToGraph(cap, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
-        if (e != cudaSuccess) {
-            rc = cuda_fail(e, "begin capture (init)");
+        vec_ctx c = make_ctx(s);
+        if ((e = cudaGraphConditionalHandleCreate(&c.loop, g, 0, 0)) != cudaSuccess) {
+            rc = cuda_fail(e, "cudaGraphConditionalHandleCreate");
             break;
         }
-        rc = enqueue_init(s, h, 1, cap);
-        // the WHILE node follows the captured init nodes
-        const cudaGraphNode_t* deps = nullptr;
-        const cudaGraphEdgeData* edges = nullptr;
-        size_t ndeps = 0;
-        cudaStreamCaptureStatus cs;
-        e = cudaStreamGetCaptureInfo(cap, &cs, nullptr, nullptr, &deps, &edges, &ndeps);
-        if (rc != DIMGPU_OK || e != cudaSuccess) {
-            cudaGraph_t dummy;
-            cudaStreamEndCapture(cap, &dummy);
-            if (rc == DIMGPU_OK)
-                rc = cuda_fail(e, "capture info");
+        c.has_loop = 1;
+        std::vector<cudaGraphNode_t> leaves;
+        if ((rc = capture_into(cap, g, {}, &leaves, [&] { return enqueue_init(s, c, cap); })) != DIMGPU_OK)
             break;
-        }
-        cudaGraphNodeParams cp = {};
-        cp.type = cudaGraphNodeTypeConditional;
-        cp.conditional.handle = h;
-        cp.conditional.type = cudaGraphCondTypeWhile;
-        cp.conditional.size = 1;
         cudaGraphNode_t wnode;
-        cudaGraph_t dummy;
-        // close the init capture, then add the WHILE node after its leaf nodes
-        std::vector<cudaGraphNode_t> leaves(deps, deps + ndeps);
-        e = cudaStreamEndCapture(cap, &dummy);
-        if (e != cudaSuccess) {
-            rc = cuda_fail(e, "end capture (init)");
+        cudaGraph_t body;
+        if ((rc = add_conditional(g, leaves, c.loop, cudaGraphCondTypeWhile, &wnode, &body)) != DIMGPU_OK)
             break;
+        if (!mixed(s)) {
+            rc = capture_into(cap, body, {}, nullptr, [&] { return enqueue_iteration(s, c, cap); });
+            if (rc != DIMGPU_OK)
+                break;
+        } else {
+            if ((e = cudaGraphConditionalHandleCreate(&c.ru, body, 0, 0)) != cudaSuccess) {
+                rc = cuda_fail(e, "cudaGraphConditionalHandleCreate (reliable update)");
+                break;
+            }
+            c.has_ru = 1;
+            std::vector<cudaGraphNode_t> ab;
+            rc = capture_into(cap, body, {}, &ab, [&]() -> int {
+                DG_CHECK(launch_spmv_f32(s->m, s->s32, s->As32, &s->cal, cg_epilogue(s), cap));
+                k_update_r_mixed<<<s->grid, kVecThreads, 0, cap>>>(s->As32, s->r32, s->s32, s->y32, s->n, c);
+                DG_CUDA(cudaGetLastError());
+                return DIMGPU_OK;
+            });
+            if (rc != DIMGPU_OK)
+                break;
+            cudaGraphNode_t inode;
+            cudaGraph_t ibody;
+            if ((rc = add_conditional(body, ab, c.ru, cudaGraphCondTypeIf, &inode, &ibody)) != DIMGPU_OK)
+                break;
+            if ((rc = capture_into(cap, ibody, {}, nullptr, [&] { return enqueue_reliable_update(s, c, cap); })) !=
+                DIMGPU_OK)
+                break;
+            rc = capture_into(cap, body, {inode}, nullptr, [&]() -> int {
+                k_update_s_mixed<<<s->grid, kVecThreads, 0, cap>>>(s->s32, s->r32, s->n, s->st);
+                DG_CUDA(cudaGetLastError());
+                return DIMGPU_OK;
+            });
+            if (rc != DIMGPU_OK)
+                break;
         }
-        e = cudaGraphAddNode(&wnode, g, leaves.data(), nullptr, leaves.size(), &cp);
-        if (e != cudaSuccess) {
-            rc = cuda_fail(e, "add WHILE node");
-            break;
-        }
-        cudaGraph_t body = cp.conditional.phGraph_out[0];
-        e = cudaStreamBeginCaptureToGraph(cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
-        if (e != cudaSuccess) {
-            rc = cuda_fail(e, "begin capture (body)");
-            break;
-        }
-        rc = enqueue_iteration(s, h, 1, cap);
-        e = cudaStreamEndCapture(cap, &dummy);
-        if (rc != DIMGPU_OK)
-            break;
-        if (e != cudaSuccess) {
-            rc = cuda_fail(e, "end capture (body)");
-            break;
-        }
-        e = cudaGraphInstantiate(&s->exec, g, 0);
-        if (e != cudaSuccess) {
+        if ((e = cudaGraphInstantiate(&s->exec, g, 0)) != cudaSuccess) {
             rc = cuda_fail(e, "cudaGraphInstantiate");
             break;
         }
@@ -523,7 +663,6 @@ int build_graph(dimgpu_cg_solver* s, cudaStream_t stream) {
         return rc;
     }
     s->graph = g;
-    (void)stream;
     return DIMGPU_OK;
 }
 
@@ -552,7 +691,7 @@ int dimgpu_cg_create(const dimgpu_csr5* m, const dimgpu_cg_params* params, void*
     s->n = m->rows;
     const int sms = device_sm_count(m->device);
     s->grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * 2, (s->n + kVecThreads - 1) / kVecThreads));
-    const uint64_t n = std::max<uint64_t>(1, s->n);
+    const uint64_t n = std::max<uint64_t>(4, s->n);
     int rc = DIMGPU_OK;
     do {
         if ((rc = dev_alloc_n(&s->b, n)) != DIMGPU_OK) break;
@@ -562,6 +701,7 @@ int dimgpu_cg_create(const dimgpu_csr5* m, const dimgpu_cg_params* params, void*
             if ((rc = dev_alloc_n(&s->r32, n)) != DIMGPU_OK) break;
             if ((rc = dev_alloc_n(&s->s32, n)) != DIMGPU_OK) break;
             if ((rc = dev_alloc_n(&s->As32, n)) != DIMGPU_OK) break;
+            if ((rc = dev_alloc_n(&s->y32, n)) != DIMGPU_OK) break;
             if ((rc = ensure_vals32(m, st)) != DIMGPU_OK) break;
         } else {
             if ((rc = dev_alloc_n(&s->r, n)) != DIMGPU_OK) break;
@@ -581,7 +721,7 @@ int dimgpu_cg_create(const dimgpu_csr5* m, const dimgpu_cg_params* params, void*
             rc = cuda_fail(cudaGetLastError(), "cudaEventCreate");
             break;
         }
-        if (params->use_graph && (rc = build_graph(s, st)) != DIMGPU_OK) break;
+        if (params->use_graph && (rc = build_graph(s)) != DIMGPU_OK) break;
     } while (false);
     if (rc != DIMGPU_OK) {
         solver_free(s);
@@ -607,21 +747,21 @@ int dimgpu_cg_solve(dimgpu_cg_solver* s, const double* b, double* x, dimgpu_cg_s
     init.thresh2 = s->params.tol * s->params.tol;
     init.max_it = s->params.max_it;
     init.delta2 = s->params.reliable_delta * s->params.reliable_delta;
-    init.alpha = init.beta = 0;
     DG_CUDA(cudaMemcpyAsync(s->st, &init, sizeof(init), cudaMemcpyHostToDevice, st));
     DG_CUDA(cudaMemsetAsync(s->cal.status, 0, sizeof(uint32_t), st));
     DG_CUDA(cudaEventRecord(s->ev0, st));
     if (s->exec) {
         DG_CUDA(cudaGraphLaunch(s->exec, st));
     } else {
-        DG_CHECK(enqueue_init(s, 0, 0, st));
+        const vec_ctx c = make_ctx(s);
+        DG_CHECK(enqueue_init(s, c, st));
         // host-driven loop: kernels turn into no-ops once the device state says stop; the host
         // looks at the state every `check` iterations
         const int64_t check = 16;
         int64_t it = 0;
         while (true) {
             for (int64_t k = 0; k < check; ++k)
-                DG_CHECK(enqueue_iteration(s, 0, 0, st));
+                DG_CHECK(enqueue_iteration(s, c, st));
             it += check;
             uint32_t stop = 0;
             DG_CUDA(cudaMemcpyAsync(&stop, &s->st->stop, sizeof(stop), cudaMemcpyDeviceToHost, st));
@@ -630,6 +770,8 @@ int dimgpu_cg_solve(dimgpu_cg_solver* s, const double* b, double* x, dimgpu_cg_s
                 break;
         }
     }
+    if (mixed(s))  // whatever y still holds (it is empty after a reliable update)
+        k_flush_mixed<<<s->grid, kVecThreads, 0, st>>>(s->x, s->y32, n, s->st, 0);
     DG_CUDA(cudaEventRecord(s->ev1, st));
     DG_CUDA(cudaMemcpyAsync(x, s->x, sizeof(double) * n, cudaMemcpyDefault, st));
     cg_state fin{};
@@ -656,13 +798,15 @@ int dimgpu_cg_solve(dimgpu_cg_solver* s, const double* b, double* x, dimgpu_cg_s
         stats->iterations = fin.iter;
         stats->reliable_updates = fin.ru_count;
         stats->rel_residual = std::sqrt(norms[0]) / bn;
-        const double rrc = s->params.precision == DIMGPU_CG_MIXED ? fin.rr_true : fin.rr;
+        const double rrc = mixed(s) ? fin.rr_true : fin.rr;
         stats->recurrence_rel_residual = std::sqrt(std::max(0.0, rrc)) / bn;
         stats->seconds = ms * 1e-3;
         stats->status = status;
     }
     if (status == DIMGPU_ERR_NOT_CONVERGED)
         set_error("CG reached max_it = %lld before tol", (long long)s->params.max_it);
+    else if (status == DIMGPU_ERR_BREAKDOWN)
+        set_error("CG breakdown: s.As <= 0 or not finite (is the matrix SPD?)");
     return status;
 }
 

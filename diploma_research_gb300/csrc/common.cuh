@@ -143,6 +143,51 @@ __device__ __forceinline__ float ldg_keep<float>(const float* p) {
 
 __device__ __forceinline__ uint32_t ldg_u32(const uint32_t* p) { return __ldg(p); }
 
+// Gathered-vector loads: read-only path, kept in L1 and (by `policy`) in L2.
+__device__ __forceinline__ double ldg_x(const double* p, uint64_t policy) {
+    double v;
+    asm("ld.global.nc.L1::evict_last.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(policy));
+    return v;
+}
+__device__ __forceinline__ float ldg_x(const float* p, uint64_t policy) {
+    float v;
+    asm("ld.global.nc.L1::evict_last.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(policy));
+    return v;
+}
+
+// Stores that the next kernel will read: kept in L2 by `policy`.
+__device__ __forceinline__ void st_keep(double* p, double v, uint64_t policy) {
+    asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(v), "l"(policy) : "memory");
+}
+__device__ __forceinline__ void st_keep(float* p, float v, uint64_t policy) {
+    asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(policy) : "memory");
+}
+
+// 16-byte vector loads/stores of the CG vectors with an L2 policy.  The loads carry no memory
+// clobber so that independent loads can be batched; callers never load an element after storing it
+// in the same kernel.
+__device__ __forceinline__ double2 ld2_keep(const double* p, uint64_t policy) {
+    double2 v;
+    asm("ld.global.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(p), "l"(policy));
+    return v;
+}
+__device__ __forceinline__ void st2_keep(double* p, double2 v, uint64_t policy) {
+    asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;" ::"l"(p), "d"(v.x), "d"(v.y), "l"(policy)
+                 : "memory");
+}
+__device__ __forceinline__ float4 ld4_keep(const float* p, uint64_t policy) {
+    float4 v;
+    asm("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "l"(p), "l"(policy));
+    return v;
+}
+__device__ __forceinline__ void st4_keep(float* p, float4 v, uint64_t policy) {
+    asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z),
+                 "f"(v.w), "l"(policy)
+                 : "memory");
+}
+
 // ------------------------------------------------------------------------------------------------
 // Warp helpers.
 // ------------------------------------------------------------------------------------------------

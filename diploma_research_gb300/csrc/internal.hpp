@@ -83,7 +83,8 @@ struct dimgpu_csr5 {
     float* vals32 = nullptr;       // f32 values in the device layout (built on first f32 use)
     uint64_t device_bytes = 0;
 
-    dimgpu::spmv_plan plan;
+    dimgpu::spmv_plan plan;    // f64 SpMV launch
+    dimgpu::spmv_plan plan32;  // f32 SpMV launch (more warps per CTA)
     dimgpu_calibrator* own_cal = nullptr;
 };
 
@@ -95,7 +96,8 @@ int convert_csr5(dimgpu_csr5* m, const uint32_t* d_row_ptr, const uint32_t* d_co
 int ensure_vals32(const dimgpu_csr5* m, cudaStream_t stream);
 
 // spmv.cu
-spmv_plan make_spmv_plan(uint64_t tiles, int sms);
+spmv_plan make_spmv_plan(uint64_t tiles, int sms, int warps_per_cta);
+spmv_plan make_spmv_plan32(uint64_t tiles, int sms);
 int prepare_spmv_kernels();
 int calibrator_init(dimgpu_calibrator* c, const dimgpu_csr5* m);
 void calibrator_release(dimgpu_calibrator* c);

@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
     using Word = typename G::Word;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint32_t s_last;
-    __shared__ double s_red[WPC * 32];
+    __shared__ double s_red[WPC];
 
     if (p.halt && *reinterpret_cast<volatile const uint32_t*>(p.halt))
         return;  // a previous stage of a CG iteration has already stopped the solve
@@ -167,6 +167,7 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
     if (t_begin < t_end) {
         const Word* gdesc = reinterpret_cast<const Word*>(p.desc);
         const uint64_t pol = policy_evict_first();
+        const uint64_t pol_keep = policy_evict_last();
         if (lane == 0) {
             for (int s = 0; s < STAGES; ++s)
                 mbar_init(&bars[s], 1);
@@ -184,34 +185,51 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
             for (int s = 0; s < STAGES && t_begin + s < t_end; ++s)
                 issue(s, t_begin + s);
 
-        uint32_t raw_next = __ldg(&p.tile_ptr[t_begin]);
+        // tile_ptr runs two tiles ahead so that no tile waits on its load
+        uint32_t raw_cur = __ldg(&p.tile_ptr[t_begin]);
+        uint32_t raw_next = __ldg(&p.tile_ptr[t_begin + 1]);
         uint64_t i = 0;
         bool failed = false;
         for (uint64_t t = t_begin; t < t_end; ++t, ++i) {
             const int s = (int)(i % STAGES);
             const uint32_t par = (uint32_t)((i / STAGES) & 1);
-            const uint32_t raw = raw_next;
-            raw_next = __ldg(&p.tile_ptr[t + 1]);
+            const uint32_t raw = raw_cur;
             const uint32_t row_stop = raw_next & ~kDirty;
             const uint32_t row_start = raw & ~kDirty;
+            raw_cur = raw_next;
+            raw_next = (t + 2 <= p.T) ? __ldg(&p.tile_ptr[t + 2]) : 0u;
             if (!mbar_wait_bounded(&bars[s], par, p.status)) {
                 failed = true;
                 break;
             }
-            const unsigned char* st = ring + (size_t)s * G::STAGE;
+            unsigned char* st = ring + (size_t)s * G::STAGE;
             const Word* sd = reinterpret_cast<const Word*>(st + G::VBYTES + G::CBYTES);
 
             VT v[SIGMA];
             uint32_t ci[SIGMA];
             load_column<VT, SIGMA>(st, lane, v, ci);
+            const Word w = sd[lane];
             VT xv[SIGMA];
 #pragma unroll
             for (int r = 0; r < SIGMA; ++r)
-                xv[r] = ldg_keep(p.x + ci[r]);
-
-            const Word w = sd[lane];
+                xv[r] = ldg_x(p.x + ci[r], pol_keep);
+            // the fused dot needs x at this tile's rows: fetch them now, off the write-out's path
+            VT xrow = VT(0);
+            if constexpr (DOT) {
+                if (row_start + lane < p.rows)
+                    xrow = ldg_x(p.x + row_start + lane, pol_keep);
+            }
             const uint32_t flag = (uint32_t)((uint64_t(w) >> (G::F.yb + G::F.sb)) & G::FMASK);
             const bool capped = (__shfl_sync(kFull, flag, 0) & 1u) != 0;
+            // Every lane now holds its column: the value area of the stage becomes the staging
+            // buffer of this tile's segment sums (slot = segment index, at most sigma*32 of them).
+            __syncwarp();
+            VT* ystage = reinterpret_cast<VT*>(st);
+            const bool dirty = (raw & kDirty) != 0;
+            const uint32_t optr = dirty ? __ldg(&p.tdo_ptr[t]) : 0u;
+            auto row_of = [&](uint32_t idx) -> uint32_t {
+                return row_start + (dirty ? __ldg(&p.tdo[optr + idx]) : idx);
+            };
 
             VT H, Lt;
             uint32_t K, row_last;
@@ -229,40 +247,27 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
                 const uint32_t yoff = (uint32_t)(uint64_t(w) & G::YMASK);
                 const uint32_t fl = flag | (lane == 0 ? 1u : 0u);
                 const uint32_t present = __ballot_sync(kFull, fl != 0);
-                const bool dirty = (raw & kDirty) != 0;
-                const uint32_t optr = dirty ? __ldg(&p.tdo_ptr[t]) : 0u;
-                auto row_of = [&](uint32_t idx) -> uint32_t {
-                    return row_start + (dirty ? __ldg(&p.tdo[optr + idx]) : idx);
-                };
 
-                VT sum = VT(0), red = VT(0), head_val = VT(0);
+                // Segments of this column: segment yoff + k is staged at slot[k].  Branch-free: a
+                // row start closes the open segment (predicated store) and restarts the sum.
+                VT* slot = ystage + yoff;
+                VT sum = VT(0), red = VT(0);
                 uint32_t k = 0;
                 bool seen = false;
 #pragma unroll
                 for (int r = 0; r < SIGMA; ++r) {
-                    if ((fl >> r) & 1u) {
-                        if (seen) {
-                            const uint32_t idx = yoff + k;
-                            if (idx == 0) {
-                                head_val = sum;
-                            } else {
-                                const uint32_t row = row_of(idx);
-                                p.y[row] = sum;
-                                if constexpr (DOT)
-                                    dot_acc += (double)sum * (double)ldg_keep(p.x + row);
-                            }
-                            ++k;
-                        } else {
-                            red = sum;
-                            seen = true;
-                        }
-                        sum = VT(0);
-                    }
+                    const bool bit = ((fl >> r) & 1u) != 0;
+                    const bool close = bit && seen;
+                    if (close)
+                        slot[k] = sum;
+                    k += close ? 1u : 0u;
+                    red = (bit && !seen) ? sum : red;
+                    seen = seen || bit;
+                    sum = bit ? VT(0) : sum;
                     sum = fma(v[r], xv[r], sum);
                 }
                 const VT L = seen ? sum : VT(0);
-                if (!seen)
-                    red = sum;
+                red = seen ? red : sum;
 
                 // segmented suffix sums of the red parts, terminated by columns with a row start
                 VT U = red;
@@ -280,27 +285,20 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
                 const VT seg_total = L + (lane == 31 ? VT(0) : nxt);
                 const uint32_t last_lane = 31u - __clz(present);
                 const bool is_present = ((present >> lane) & 1u) != 0;
-                const uint32_t last_idx = yoff + k;
+                if (is_present && lane != last_lane)
+                    slot[k] = seg_total;  // the column's open segment, closed by a later column
                 uint32_t my_row_last = 0;
-                if (is_present && lane != last_lane) {
-                    if (last_idx == 0) {
-                        head_val = seg_total;
-                    } else {
-                        const uint32_t row = row_of(last_idx);
-                        p.y[row] = seg_total;
-                        if constexpr (DOT)
-                            dot_acc += (double)seg_total * (double)ldg_keep(p.x + row);
-                    }
-                } else if (lane == last_lane) {
-                    my_row_last = row_of(last_idx);
-                }
-                K = __shfl_sync(kFull, last_idx + 1, last_lane);
+                if (lane == last_lane)
+                    my_row_last = row_of(yoff + k);
+                K = __shfl_sync(kFull, yoff + k + 1, last_lane);
                 Lt = __shfl_sync(kFull, seg_total, last_lane);
                 row_last = __shfl_sync(kFull, my_row_last, last_lane);
-                H = (K == 1) ? Lt : __shfl_sync(kFull, head_val, 0);
+                __syncwarp();
+                H = (K == 1) ? Lt : ystage[0];  // segment 0 sits in slot 0 whenever it closed in this tile
             }
 
             // in-order carry chain over the warp's tiles (uniform across lanes)
+            bool head_staged = false;
             if (K == 1) {
                 if (capped) {
                     if (open)
@@ -316,12 +314,12 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
                     cal_valid = true;
                 }
             } else {
-                if (capped) {
-                    if (open)
+                if (capped || open) {
+                    if (capped && open)
                         write_row_lane0(carry_row, carry);
-                    write_row_lane0(row_start, H);
-                } else if (open) {
-                    write_row_lane0(row_start, carry + H);
+                    if (!capped && lane == 0)
+                        ystage[0] = carry + H;  // the row that began before this tile closes here
+                    head_staged = true;
                 } else {
                     cal += H;
                     cal_row = row_start;
@@ -330,6 +328,24 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
                 open = true;
                 carry = Lt;
                 carry_row = row_last;
+            }
+            // write the tile's closed rows coalesced (slots 0 or 1 .. K-2; slot K-1 is the carry)
+            __syncwarp();
+            if (K > 1) {
+                const uint32_t lo = head_staged ? 0u : 1u;
+                VT xfirst = VT(0);
+                if constexpr (DOT)
+                    xfirst = __shfl_down_sync(kFull, xrow, lo);  // x[row_start + lo + lane]
+                for (uint32_t j = lo + lane; j + 1 < K; j += 32) {
+                    const VT val = ystage[j];
+                    const uint32_t row = row_of(j);
+                    st_keep(p.y + row, val, pol_keep);
+                    if constexpr (DOT) {
+                        const bool have = !dirty && j == lo + lane && lane + lo < 32;
+                        const VT xr = have ? xfirst : ldg_x(p.x + row, pol_keep);
+                        dot_acc = fma((double)val, (double)xr, dot_acc);
+                    }
+                }
             }
 
             __syncwarp();
@@ -410,15 +426,15 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
         double part = fix_dot;
         for (uint32_t wi = threadIdx.x; wi < p.nwarps; wi += blockDim.x)
             part += __ldcg(&p.dot_part[wi]);
-        s_red[threadIdx.x] = part;
+        // warp sums, then the WPC warp sums in order (any block size; fixed order)
+        part = warp_sum(part);
+        if (lane == 0)
+            s_red[warp] = part;
         __syncthreads();
-        for (int h = WPC * 16; h > 0; h >>= 1) {
-            if ((int)threadIdx.x < h)
-                s_red[threadIdx.x] += s_red[threadIdx.x + h];
-            __syncthreads();
-        }
         if (threadIdx.x == 0) {
-            const double dot = s_red[0];
+            double dot = 0.0;
+            for (int wi = 0; wi < WPC; ++wi)
+                dot += s_red[wi];
             if (p.dot_out)
                 *p.dot_out = dot;
             if (p.rr) {
@@ -447,7 +463,9 @@ template <typename VT, int SIGMA, int WPC, int STAGES, bool DOT>
 int launch_cfg(const dimgpu_csr5* m, const VT* vals, const VT* x, VT* y, dimgpu_calibrator* cal,
                const spmv_epilogue& ep, cudaStream_t stream) {
     constexpr size_t smem = smem_bytes<VT, SIGMA, WPC, STAGES>();
-    const spmv_plan& pl = m->plan;
+    const spmv_plan& pl = sizeof(VT) == 8 ? m->plan : m->plan32;
+    if (pl.warps_per_cta != WPC)
+        return fail(DIMGPU_ERR_UNSUPPORTED, "launch plan has %d warps per CTA, kernel %d", pl.warps_per_cta, WPC);
     if (pl.nwarps > cal->nslots)
         return fail(DIMGPU_ERR_INVALID_ARGUMENT, "calibrator has %u slots, plan needs %u", cal->nslots, pl.nwarps);
     spmv_params<VT> p;
@@ -481,7 +499,8 @@ int launch_cfg(const dimgpu_csr5* m, const VT* vals, const VT* x, VT* y, dimgpu_
     return DIMGPU_OK;
 }
 
-constexpr int kWPC = 16;
+constexpr int kWPC = 16;    // f64: 16 warps x 2 stages x 6.3 KB per SM (register-limited)
+constexpr int kWPC32 = 24;  // f32: 24 warps x 2 stages x 4.2 KB per SM
 constexpr int kStages = 2;
 
 template <typename VT, int SIGMA, int WPC, int STAGES, bool DOT>
@@ -500,8 +519,8 @@ int prepare_spmv_kernels() {
         return DIMGPU_OK;
     DG_CUDA((set_smem_attr<double, 16, kWPC, kStages, false>()));
     DG_CUDA((set_smem_attr<double, 16, kWPC, kStages, true>()));
-    DG_CUDA((set_smem_attr<float, 16, kWPC, kStages, false>()));
-    DG_CUDA((set_smem_attr<float, 16, kWPC, kStages, true>()));
+    DG_CUDA((set_smem_attr<float, 16, kWPC32, kStages, false>()));
+    DG_CUDA((set_smem_attr<float, 16, kWPC32, kStages, true>()));
     done = 1;
     return DIMGPU_OK;
 }
@@ -513,26 +532,28 @@ int device_sm_count(int device) {
     return sms;
 }
 
-spmv_plan make_spmv_plan(uint64_t tiles, int sms) {
+spmv_plan make_spmv_plan(uint64_t tiles, int sms, int wpc) {
     spmv_plan pl;
-    pl.warps_per_cta = kWPC;
-    const uint64_t max_warps = (uint64_t)sms * kWPC;
+    pl.warps_per_cta = wpc;
+    const uint64_t max_warps = (uint64_t)sms * wpc;
     uint64_t warps = std::min<uint64_t>(max_warps, std::max<uint64_t>(1, tiles));
-    pl.grid = (int)((warps + kWPC - 1) / kWPC);
-    pl.nwarps = (uint32_t)pl.grid * kWPC;
+    pl.grid = (int)((warps + wpc - 1) / wpc);
+    pl.nwarps = (uint32_t)pl.grid * wpc;
     pl.tiles_per_warp = tiles ? (tiles + pl.nwarps - 1) / pl.nwarps : 0;
     // shrink the grid when the last CTAs would have no tiles
     if (pl.tiles_per_warp) {
         const uint64_t used_warps = (tiles + pl.tiles_per_warp - 1) / pl.tiles_per_warp;
-        pl.grid = (int)((used_warps + kWPC - 1) / kWPC);
-        pl.nwarps = (uint32_t)pl.grid * kWPC;
+        pl.grid = (int)((used_warps + wpc - 1) / wpc);
+        pl.nwarps = (uint32_t)pl.grid * wpc;
     }
     return pl;
 }
 
+spmv_plan make_spmv_plan32(uint64_t tiles, int sms) { return make_spmv_plan(tiles, sms, kWPC32); }
+
 int calibrator_init(dimgpu_calibrator* c, const dimgpu_csr5* m) {
     cudaGetDevice(&c->device);
-    c->nslots = std::max<uint32_t>(m->plan.nwarps, 1);
+    c->nslots = std::max<uint32_t>(std::max(m->plan.nwarps, m->plan32.nwarps), 1);
     DG_CHECK(dev_alloc_n(&c->cal_val, c->nslots));
     DG_CHECK(dev_alloc_n(&c->cal_row, c->nslots));
     DG_CHECK(dev_alloc_n(&c->dot_part, c->nslots + 1));
@@ -574,8 +595,8 @@ int launch_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calib
     const bool dot = ep.dot_out || ep.alpha_out;
     switch (m->sigma) {
     case 16:
-        return dot ? launch_cfg<float, 16, kWPC, kStages, true>(m, m->vals32, x, y, cal, ep, stream)
-                   : launch_cfg<float, 16, kWPC, kStages, false>(m, m->vals32, x, y, cal, ep, stream);
+        return dot ? launch_cfg<float, 16, kWPC32, kStages, true>(m, m->vals32, x, y, cal, ep, stream)
+                   : launch_cfg<float, 16, kWPC32, kStages, false>(m, m->vals32, x, y, cal, ep, stream);
     default:
         return fail(DIMGPU_ERR_UNSUPPORTED, "sigma %u has no SpMV kernel", m->sigma);
     }

@@ -104,6 +104,11 @@ DIMGPU_API int dimgpu_calibrator_destroy(dimgpu_calibrator* c);
  * elements, y rows elements, both device memory.  Requires a device-layout matrix (omega = 32). */
 DIMGPU_API int dimgpu_csr5_spmv(const dimgpu_csr5* m, const double* x, double* y, dimgpu_calibrator* cal, void* stream);
 
+/* y := A x and *dot := x.y = x'Ax (the energy product CG needs) in one pass, for a square matrix.
+ * dot is device memory; the sum is taken in a fixed order (bit-reproducible). */
+DIMGPU_API int dimgpu_csr5_spmv_dot(const dimgpu_csr5* m, const double* x, double* y, double* dot,
+                                    dimgpu_calibrator* cal, void* stream);
+
 /* The same product with host x and y: copies x in, multiplies, copies y out, synchronizes. */
 DIMGPU_API int dimgpu_csr5_spmv_host(const dimgpu_csr5* m, const double* x_host, double* y_host);
 

@@ -134,6 +134,31 @@ def test_f32_spmv(native, torch_cuda):
     assert_spmv_close(yd.cpu().numpy().astype(np.float64), y_ref, ax, SPMV_RTOL_F32 * 50)
 
 
+@pytest.mark.parametrize("seed", range(3))
+def test_spmv_dot_fused(native, torch_cuda, seed):
+    """y = A x with x.y from the same pass (the CG energy product), against numpy."""
+    import ctypes
+
+    from diploma_research_gb300 import _native as N
+
+    torch = torch_cuda
+    rng = np.random.default_rng(40 + seed)
+    n = int(rng.integers(1000, 60000))
+    m = random_csr(rng, n, n, float(rng.uniform(2, 40)), empty_frac=0.05, long_rows=3, long_len=(2000, 20000))
+    A = csr5.from_csr(m)
+    x = rng.uniform(-1, 1, n)
+    xd = torch.tensor(x, device="cuda", dtype=torch.float64)
+    yd = torch.full((n,), float("nan"), device="cuda", dtype=torch.float64)
+    dot = torch.zeros(1, device="cuda", dtype=torch.float64)
+    N.check(native.dimgpu_csr5_spmv_dot(A._h, xd.data_ptr(), yd.data_ptr(), dot.data_ptr(), None, None))
+    torch.cuda.synchronize()
+    y_ref, ax = _refs(m, x)
+    assert_spmv_close(yd.cpu().numpy(), y_ref, ax, SPMV_RTOL_F64)
+    ref = float(np.dot(x, y_ref))
+    scale = float(np.dot(np.abs(x), ax))
+    assert abs(float(dot.item()) - ref) <= 1e-12 * scale
+
+
 def test_linearity(native, torch_cuda):
     rng = np.random.default_rng(8)
     m = random_csr(rng, 6000, 6000, 15.0, long_rows=3, long_len=(1000, 5000))
