@@ -397,6 +397,64 @@ def run_spmv_only(args):
     return 0
 
 
+def run_batch(args):
+    """Multi-RHS workload: 3-D 7-point Laplacian 192^3 (n = 7,077,888), k right-hand sides b_j = A x*_j
+    (x* ~ U[-1,1], seed 3), block CG to 1e-10 per column in FP64 and mixed precision, against k separate
+    FP64 solves (timed on two columns and scaled by k/2).  Prints one JSON line per k."""
+    import numpy as np
+    import torch
+
+    from diploma_research_gb300 import build as B
+
+    B.build()
+    from diploma_research_gb300.cg import BlockCGSolver, CGSolver
+    from diploma_research_gb300.csr5 import csr5
+    from diploma_research_gb300.generators import WORKLOADS, rhs
+
+    m = WORKLOADS["lap3d7_192"]["build"]()
+    n = m.dimensions.rows
+    A = csr5.from_csr(m)
+    stream = torch.cuda.current_stream()
+    single = CGSolver(A, tol=TOL, precision="fp64", stream=stream)
+    for k in [int(v) for v in args.batch.split(",")]:
+        xs, Bh = rhs(m, 3, k=k)
+        Bd = torch.tensor(Bh, device="cuda", dtype=torch.float64)
+        out = {"workload": f"lap3d7_192: 3-D 7-point Laplacian 192^3, n={n}, nnz={m.nnz}, k={k}, CG to {TOL:g}"}
+        for prec in ("fp64", "mixed"):
+            s = BlockCGSolver(A, k, tol=TOL, precision=prec, stream=stream, use_graph=not args.no_graph)
+            Xd = torch.zeros((n, k), device="cuda", dtype=torch.float64)
+            s.solve(Bd, Xd, stream=stream)  # warm-up
+            Xd.zero_()
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            _, res = s.solve(Bd, Xd, stream=stream)
+            torch.cuda.synchronize()
+            sec = time.perf_counter() - t
+            err = float(np.linalg.norm(Xd.cpu().numpy() - xs) / np.linalg.norm(xs))
+            out[prec] = {"seconds": sec, "rhs_solves_per_s": k / sec, "iterations": res.iterations,
+                         "converged_columns": res.converged_columns, "max_rel_residual": res.max_rel_residual,
+                         "reliable_updates": res.reliable_updates, "rel_error_vs_xstar": err}
+            del s
+        sep = []
+        for j in range(min(2, k)):
+            b = torch.tensor(np.ascontiguousarray(Bh[:, j]), device="cuda", dtype=torch.float64)
+            x = torch.zeros(n, device="cuda", dtype=torch.float64)
+            single.solve(b, x, stream=stream)
+            x.zero_()
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            _, r1 = single.solve(b, x, stream=stream)
+            torch.cuda.synchronize()
+            sep.append((time.perf_counter() - t, r1.iterations))
+        sep_s = statistics.mean(v[0] for v in sep) * k
+        out["separate_fp64"] = {"seconds": sep_s, "rhs_solves_per_s": k / sep_s,
+                                "iterations": [v[1] for v in sep], "note": "two columns timed, scaled to k"}
+        out["speedup_block_fp64"] = sep_s / out["fp64"]["seconds"]
+        out["speedup_block_mixed"] = sep_s / out["mixed"]["seconds"]
+        print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -408,7 +466,10 @@ def main():
     ap.add_argument("--f32", action="store_true", help="with --spmv-only: the f32 product")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven CG loop instead of the CUDA graph (profilers list every kernel)")
+    ap.add_argument("--batch", default=None, help="comma-separated k: the multi-RHS block-CG workload")
     args = ap.parse_args()
+    if args.batch:
+        return run_batch(args)
     if args.spmv_only:
         return run_spmv_only(args)
     if args.warmup < 3:

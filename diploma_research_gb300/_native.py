@@ -57,6 +57,12 @@ class cg_stats(ctypes.Structure):
                 ("seconds", ctypes.c_double), ("status", ctypes.c_int32)]
 
 
+class block_cg_stats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int64), ("reliable_updates", ctypes.c_int64),
+                ("max_rel_residual", ctypes.c_double), ("seconds", ctypes.c_double),
+                ("converged_columns", ctypes.c_int32), ("status", ctypes.c_int32)]
+
+
 class DimgpuError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"dimgpu error {code}: {msg}")
@@ -94,6 +100,9 @@ _SIGNATURES = {
     "dimgpu_csr5_spmv_host": [_vp, _vp, _vp],
     "dimgpu_csr5_spmv_dot": [_vp, _vp, _vp, _vp, _vp, _vp],
     "dimgpu_csr5_spmv_f32": [_vp, _vp, _vp, _vp, _vp],
+    "dimgpu_csr5_spmm": [_vp, _u32, _vp, _u64, _vp, _u64, _vp],
+    "dimgpu_csr5_spmm_f32": [_vp, _u32, _vp, _u64, _vp, _u64, _vp],
+    "dimgpu_csr5_spmm_shape": [_vp, _u32, ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
     "dimgpu_vec_axpy": [_u64, _f64, _vp, _vp, _vp],
     "dimgpu_vec_aypx": [_u64, _f64, _vp, _vp, _vp],
     "dimgpu_vec_set": [_u64, _f64, _vp, _vp],
@@ -102,6 +111,9 @@ _SIGNATURES = {
     "dimgpu_cg_destroy": [_vp],
     "dimgpu_cg_solve": [_vp, _vp, _vp, ctypes.POINTER(cg_stats), _vp],
     "dimgpu_cg_solve_host": [_vp, _vp, _vp, ctypes.POINTER(cg_stats)],
+    "dimgpu_block_cg_create": [_vp, _u32, ctypes.POINTER(cg_params), _vp, ctypes.POINTER(_vp)],
+    "dimgpu_block_cg_destroy": [_vp],
+    "dimgpu_block_cg_solve": [_vp, _vp, _u64, _vp, _u64, ctypes.POINTER(block_cg_stats), _vp, _vp, _vp],
     "dimgpu_version": [],
 }
 

@@ -77,3 +77,56 @@ def cg(A: csr5, b, x0=None, tol: float = 1e-10, max_it: int = 100000, precision:
        use_graph: bool = True):
     """One-shot solve: returns (x, cg_result)."""
     return CGSolver(A, tol=tol, max_it=max_it, precision=precision, use_graph=use_graph).solve(b, x0)
+
+
+@dataclass
+class block_cg_result:
+    iterations: int               # iterations of the slowest column
+    reliable_updates: int
+    max_rel_residual: float
+    seconds: float
+    converged_columns: int
+    col_iterations: list
+    col_rel_residual: list
+
+
+class BlockCGSolver:
+    """k <= 32 simultaneous CG solves sharing one CSR5 SpMM per iteration, per-column convergence masks.
+
+    solve(B, X) takes device arrays of shape (n, k) (float64, row-major); X holds the initial guesses and
+    receives the solutions."""
+
+    def __init__(self, A: csr5, k: int, tol: float = 1e-10, max_it: int = 100000, precision: str = "fp64",
+                 use_graph: bool = True, reliable_delta: float = 0.1, stream=None):
+        if precision not in _PREC:
+            raise ValueError(f"precision must be one of {sorted(_PREC)}")
+        self.A, self.k = A, int(k)
+        self.params = N.cg_params(float(tol), int(max_it), _PREC[precision], 1 if use_graph else 0,
+                                  float(reliable_delta))
+        h = ctypes.c_void_p()
+        N.check(N.lib().dimgpu_block_cg_create(A._h, self.k, ctypes.byref(self.params), N.stream_ptr(stream),
+                                               ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            N.lib().dimgpu_block_cg_destroy(h)
+            self._h = None
+
+    def solve(self, B, X, stream=None, raise_on_failure: bool = True):
+        n = self.A.dimensions.rows
+        for name, a in (("B", B), ("X", X)):
+            shp = a.__cuda_array_interface__["shape"]
+            if tuple(shp) != (n, self.k):
+                raise ValueError(f"{name} must have shape ({n}, {self.k}), got {tuple(shp)}")
+        st = N.block_cg_stats()
+        its = (ctypes.c_int64 * self.k)()
+        rel = (ctypes.c_double * self.k)()
+        rc = N.lib().dimgpu_block_cg_solve(self._h, N.device_ptr(B, "<f8"), self.k, N.device_ptr(X, "<f8"), self.k,
+                                           ctypes.byref(st), its, rel, N.stream_ptr(stream))
+        res = block_cg_result(int(st.iterations), int(st.reliable_updates), float(st.max_rel_residual),
+                              float(st.seconds), int(st.converged_columns), list(its), list(rel))
+        if rc != N.OK and (raise_on_failure or rc not in (N.ERR_NOT_CONVERGED, N.ERR_BREAKDOWN)):
+            N.check(rc)
+        return X, res

@@ -233,3 +233,33 @@ class csr5:
                 if name == "x":
                     raise ValueError("can't multiply, vector size doesn't match column count of the matrix")
                 raise ValueError(f"{name} has {size} elements, expected {n}")
+
+
+def spmm(A: csr5, X, Y, stream=None):
+    """Y := A X for k right-hand sides (device arrays, row-major: X cols x k, Y rows x k).  f64 or f32.
+
+    The first call for a given (k, precision) picks the fastest SpMM launch shape by timing."""
+    cx = X.__cuda_array_interface__
+    cy = Y.__cuda_array_interface__
+    if len(cx["shape"]) != 2 or len(cy["shape"]) != 2:
+        raise ValueError("X and Y must be 2-D (rows x k)")
+    n_x, k = cx["shape"]
+    n_y, k2 = cy["shape"]
+    if k != k2 or n_x != A.dimensions.cols or n_y != A.dimensions.rows:
+        raise ValueError("shape mismatch: X must be cols x k and Y rows x k")
+    typ = cx["typestr"]
+    L = N.lib()
+    if typ == "<f4":
+        N.check(L.dimgpu_csr5_spmm_f32(A._h, k, N.device_ptr(X, "<f4"), k, N.device_ptr(Y, "<f4"), k,
+                                       N.stream_ptr(stream)))
+    else:
+        N.check(L.dimgpu_csr5_spmm(A._h, k, N.device_ptr(X, "<f8"), k, N.device_ptr(Y, "<f8"), k,
+                                   N.stream_ptr(stream)))
+    return Y
+
+
+def spmm_shape(A: csr5, k: int, f32: bool = False) -> int:
+    """The autotuned SpMM launch shape for (k, precision), -1 before the first call."""
+    v = ctypes.c_int()
+    N.check(N.lib().dimgpu_csr5_spmm_shape(A._h, k, 1 if f32 else 0, ctypes.byref(v)))
+    return int(v.value)

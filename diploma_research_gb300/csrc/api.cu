@@ -129,6 +129,10 @@ using namespace dimgpu;
 static void destroy_matrix(dimgpu_csr5* m) {
     if (!m)
         return;
+    if (m->spmm_sc) {
+        spmm_scratch_release(static_cast<spmm_scratch*>(m->spmm_sc));
+        delete static_cast<spmm_scratch*>(m->spmm_sc);
+    }
     if (m->own_cal) {
         calibrator_release(m->own_cal);
         delete m->own_cal;
@@ -179,6 +183,9 @@ int dimgpu_csr5_from_csr(uint32_t rows, uint32_t cols, uint64_t nnz, const uint3
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
     dimgpu_csr5* m = new dimgpu_csr5();
+    for (auto& row : m->spmm_shape)
+        for (int& v : row)
+            v = -1;
     cudaGetDevice(&m->device);
     m->rows = rows;
     m->cols = cols;

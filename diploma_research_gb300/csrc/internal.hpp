@@ -83,6 +83,8 @@ struct dimgpu_csr5 {
     float* vals32 = nullptr;       // f32 values in the device layout (built on first f32 use)
     uint64_t device_bytes = 0;
 
+    int spmm_shape[2][33];       // autotuned SpMM launch shape per (f32?, k); -1 = not tuned yet
+    void* spmm_sc = nullptr;     // the handle's own SpMM scratch (dimgpu::spmm_scratch), built on first use
     dimgpu::spmv_plan plan;    // f64 SpMV launch
     dimgpu::spmv_plan plan32;  // f32 SpMV launch (more warps per CTA)
     dimgpu_calibrator* own_cal = nullptr;
@@ -117,6 +119,37 @@ int launch_spmv_f64(const dimgpu_csr5* m, const double* x, double* y, dimgpu_cal
 int launch_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calibrator* cal,
                     const spmv_epilogue& ep, cudaStream_t stream);
 int check_status(dimgpu_calibrator* cal, cudaStream_t stream);
+
+// spmm.cu: CSR5 SpMM (lanes = right-hand sides, one pass takes k <= 32 columns)
+constexpr int kSpmmShapes = 3;  // launch shapes the autotuner chooses from (warps per CTA x stages)
+struct spmm_args {
+    const void* X = nullptr;
+    void* Y = nullptr;
+    uint64_t ldx = 0, ldy = 0;
+    uint32_t k = 0;
+    double* dot_out = nullptr;      // block-CG epilogue: per-column X.Y
+    const double* rr = nullptr;     // and alpha_j = rr_j / dot_j for the columns in `mask`
+    double* alpha_out = nullptr;
+    const uint32_t* mask = nullptr;      // [2][32]; the half selected by *mask_sel (when given)
+    const uint32_t* mask_sel = nullptr;
+    uint32_t* halt = nullptr;
+};
+struct spmm_scratch {
+    uint32_t nslots = 0;
+    double* cal_val = nullptr;   // [nslots * 32]
+    uint32_t* cal_row = nullptr; // [nslots]
+    double* dot_part = nullptr;  // [nslots * 32]
+    uint32_t* counter = nullptr;
+    uint32_t* status = nullptr;
+};
+int prepare_spmm_kernels();
+uint32_t spmm_max_slots(const dimgpu_csr5* m);
+int spmm_scratch_init(spmm_scratch* s, const dimgpu_csr5* m);
+void spmm_scratch_release(spmm_scratch* s);
+int launch_spmm(const dimgpu_csr5* m, bool f32, const spmm_args& a, const spmm_scratch& sc, int shape,
+                cudaStream_t st);
+int autotune_spmm(const dimgpu_csr5* m, bool f32, const spmm_args& a, const spmm_scratch& sc, cudaStream_t st,
+                  int* best_shape, float* best_ms);
 
 // api.cu: deterministic dot product into device memory (d_part holds 256 partials)
 int dot_device(uint64_t n, const double* a, const double* b, double* d_out, double* d_part, cudaStream_t s);

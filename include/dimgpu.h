@@ -131,6 +131,20 @@ DIMGPU_API int dimgpu_csr5_spmv_f32(const dimgpu_csr5* m, const float* x, float*
  *   - x, y: device memory of the matrix's device (the current device).  The call is asynchronous. */
 DIMGPU_API int dimgpu_csr5_spmv_static_scratch(const dimgpu_csr5* m, const double* x, double* y, void* stream);
 
+/* ---- several right-hand sides ------------------------------------------------------------------- */
+
+/* Y := A X for k right-hand sides (the spec batching of csr5::spmv): X is cols x k, Y rows x k,
+ * both row-major with leading dimensions ldx, ldy >= k (device memory).  k > 32 runs in passes of 32
+ * columns.  The first call for a given (k, precision) times the candidate launch shapes on these
+ * operands and keeps the fastest (make it outside any stream capture).  Calls on one matrix must not
+ * overlap on the device (they share the matrix's SpMM scratch). */
+DIMGPU_API int dimgpu_csr5_spmm(const dimgpu_csr5* m, uint32_t k, const double* X, uint64_t ldx, double* Y,
+                                uint64_t ldy, void* stream);
+DIMGPU_API int dimgpu_csr5_spmm_f32(const dimgpu_csr5* m, uint32_t k, const float* X, uint64_t ldx, float* Y,
+                                    uint64_t ldy, void* stream);
+/* The launch shape the autotuner picked for (k, f32): 0..2, or -1 before the first call. */
+DIMGPU_API int dimgpu_csr5_spmm_shape(const dimgpu_csr5* m, uint32_t k, int f32, int* shape);
+
 /* ---- vectors (include/dim/vec.h:29-84), device memory ----------------------------------------- */
 
 DIMGPU_API int dimgpu_vec_axpy(uint64_t n, double alpha, const double* x, double* y, void* stream); /* y += a x */
@@ -168,6 +182,31 @@ DIMGPU_API int dimgpu_cg_destroy(dimgpu_cg_solver* s);
 DIMGPU_API int dimgpu_cg_solve(dimgpu_cg_solver* s, const double* b, double* x, dimgpu_cg_stats* stats, void* stream);
 /* The same with host b and x (copies in and out inside the call). */
 DIMGPU_API int dimgpu_cg_solve_host(dimgpu_cg_solver* s, const double* b_host, double* x_host, dimgpu_cg_stats* stats);
+
+/* ---- block CG: k <= 32 right-hand sides, one SpMM per iteration -------------------------------- */
+
+typedef struct dimgpu_block_cg dimgpu_block_cg;
+
+typedef struct {
+    int64_t iterations;       /* iterations of the slowest column */
+    int64_t reliable_updates; /* batched f64 residual replacements (mixed) */
+    double max_rel_residual;  /* max over columns of ||b_j - A x_j|| / ||b_j|| (f64, recomputed) */
+    double seconds;           /* device time of the solve */
+    int32_t converged_columns;
+    int32_t status;           /* DIMGPU_OK, _NOT_CONVERGED or _BREAKDOWN */
+} dimgpu_block_cg_stats;
+
+/* k simultaneous CG solves (the dim_sp recurrence per column, its own alpha_j/beta_j) sharing one
+ * CSR5 SpMM per iteration; a column stops when it converges (per-column mask).  params as for
+ * dimgpu_cg_create (precision FP64 or MIXED).  Autotunes the SpMM launch shape on creation. */
+DIMGPU_API int dimgpu_block_cg_create(const dimgpu_csr5* m, uint32_t k, const dimgpu_cg_params* params,
+                                      void* stream, dimgpu_block_cg** out);
+DIMGPU_API int dimgpu_block_cg_destroy(dimgpu_block_cg* s);
+/* B: n x k (leading dimension ldb), X: n x k initial guesses -> solutions (ldx); device memory.
+ * col_iterations / col_rel_residual: optional host arrays of k entries. */
+DIMGPU_API int dimgpu_block_cg_solve(dimgpu_block_cg* s, const double* B, uint64_t ldb, double* X, uint64_t ldx,
+                                     dimgpu_block_cg_stats* stats, int64_t* col_iterations,
+                                     double* col_rel_residual, void* stream);
 
 /* ---- diagnostics ------------------------------------------------------------------------------ */
 

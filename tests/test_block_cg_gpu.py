@@ -1,0 +1,79 @@
+"""Block CG (k simultaneous solves, one SpMM per iteration, per-column masks) against single CG."""
+import numpy as np
+import pytest
+
+from diploma_research_gb300.cg import BlockCGSolver, cg
+from diploma_research_gb300.csr5 import csr5
+from diploma_research_gb300.generators import laplacian_2d_5pt, laplacian_3d_7pt, rhs
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("k", [1, 5, 8, 16])
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_block_cg_fp64_matches_single_cg(native, torch_cuda, k, use_graph):
+    torch = torch_cuda
+    m = laplacian_2d_5pt(40)
+    n = m.dimensions.rows
+    xs, B = rhs(m, 7, k=k)
+    A = csr5.from_csr(m)
+    s = BlockCGSolver(A, k, tol=1e-10, use_graph=use_graph)
+    Bd = torch.tensor(B, device="cuda", dtype=torch.float64)
+    Xd = torch.zeros((n, k), device="cuda", dtype=torch.float64)
+    _, res = s.solve(Bd, Xd)
+    assert res.converged_columns == k and res.max_rel_residual <= 1.5e-10
+    X = Xd.cpu().numpy()
+    for j in range(k):
+        xj, rj = cg(A, B[:, j], tol=1e-10)
+        assert abs(res.col_iterations[j] - rj.iterations) <= 1, (j, res.col_iterations[j], rj.iterations)
+        np.testing.assert_allclose(X[:, j], xj, rtol=0, atol=1e-9)
+
+
+def test_block_cg_masks(native, torch_cuda):
+    """A zero column converges at once; a column started at its solution too; the others keep going."""
+    torch = torch_cuda
+    m = laplacian_2d_5pt(32)
+    n = m.dimensions.rows
+    xs, B = rhs(m, 3, k=4)
+    B[:, 1] = 0.0
+    A = csr5.from_csr(m)
+    X0 = np.zeros((n, 4))
+    X0[:, 2] = xs[:, 2]
+    s = BlockCGSolver(A, 4, tol=1e-10)
+    Bd = torch.tensor(B, device="cuda", dtype=torch.float64)
+    Xd = torch.tensor(X0, device="cuda", dtype=torch.float64)
+    _, res = s.solve(Bd, Xd)
+    assert res.converged_columns == 4
+    assert res.col_iterations[1] == 0 and res.col_iterations[2] <= 1
+    assert res.col_iterations[0] > 10 and res.col_iterations[3] > 10
+    np.testing.assert_allclose(Xd.cpu().numpy()[:, [0, 3]], xs[:, [0, 3]], atol=1e-7)
+
+
+@pytest.mark.parametrize("k", [8, 32])
+def test_block_cg_mixed(native, torch_cuda, k):
+    torch = torch_cuda
+    m = laplacian_3d_7pt(20)
+    n = m.dimensions.rows
+    xs, B = rhs(m, 11, k=k)
+    A = csr5.from_csr(m)
+    s = BlockCGSolver(A, k, tol=1e-10, precision="mixed")
+    Bd = torch.tensor(B, device="cuda", dtype=torch.float64)
+    Xd = torch.zeros((n, k), device="cuda", dtype=torch.float64)
+    _, res = s.solve(Bd, Xd)
+    assert res.converged_columns == k
+    assert res.max_rel_residual <= 1.01e-10
+    assert res.reliable_updates >= 1
+    err = np.linalg.norm(Xd.cpu().numpy() - xs) / np.linalg.norm(xs)
+    assert err < 1e-7
+
+
+def test_block_cg_not_converged(native, torch_cuda):
+    torch = torch_cuda
+    m = laplacian_2d_5pt(32)
+    n = m.dimensions.rows
+    _, B = rhs(m, 5, k=2)
+    A = csr5.from_csr(m)
+    s = BlockCGSolver(A, 2, tol=1e-14, max_it=7)
+    Xd = torch.zeros((n, 2), device="cuda", dtype=torch.float64)
+    _, res = s.solve(torch.tensor(B, device="cuda", dtype=torch.float64), Xd, raise_on_failure=False)
+    assert res.converged_columns == 0 and res.iterations == 7

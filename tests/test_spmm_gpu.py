@@ -1,0 +1,70 @@
+"""CSR5 SpMM (k right-hand sides) through the C ABI against a CSR reference, f64 and f32."""
+import numpy as np
+import pytest
+
+from diploma_research_gb300.csr5 import csr5, spmm, spmm_shape
+from helpers import csr_from_lengths, random_csr
+
+pytestmark = pytest.mark.gpu
+
+
+def _check(torch, m, k, seed=0, f32=False):
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(-1, 1, (m.dimensions.cols, k))
+    S = m.to_scipy()
+    Y_ref = S @ X
+    AX = abs(S) @ np.abs(X)
+    A = csr5.from_csr(m)
+    dt = torch.float32 if f32 else torch.float64
+    Xd = torch.tensor(X, device="cuda", dtype=dt)
+    Yd = torch.full((m.dimensions.rows, k), float("nan"), device="cuda", dtype=dt)
+    spmm(A, Xd, Yd)
+    torch.cuda.synchronize()
+    Y = Yd.cpu().numpy().astype(np.float64)
+    if f32:
+        Y_ref = S @ X.astype(np.float32).astype(np.float64)
+    tol = 1e-4 if f32 else 1e-12
+    err = np.abs(Y - Y_ref)
+    assert np.all(err <= tol * AX + 1e-300), float(np.max(err / (AX + 1e-300)))
+    assert spmm_shape(A, min(k, 32), f32) in (0, 1, 2)
+    return A
+
+
+@pytest.mark.parametrize("k", [1, 3, 8, 16, 32, 40])
+def test_spmm_random(native, torch_cuda, k):
+    rng = np.random.default_rng(k)
+    m = random_csr(rng, 5000, 4000, 12.0, empty_frac=0.1, long_rows=3, long_len=(700, 3000))
+    _check(torch_cuda, m, k, seed=k)
+
+
+@pytest.mark.parametrize("k", [8, 32])
+def test_spmm_f32(native, torch_cuda, k):
+    rng = np.random.default_rng(100 + k)
+    m = random_csr(rng, 3000, 3000, 9.0, empty_frac=0.05, long_rows=2, long_len=(600, 2000))
+    _check(torch_cuda, m, k, seed=k, f32=True)
+
+
+@pytest.mark.parametrize("lens,cols", [([3, 0, 5, 1], 10), ([0, 0, 0], 4), ([20000], 20000),
+                                       ([0] * 50 + [512] + [0] * 50, 600), ([1] * 4096, 3)])
+def test_spmm_edge_cases(native, torch_cuda, lens, cols):
+    rng = np.random.default_rng(len(lens))
+    m = csr_from_lengths(lens, cols, rng)
+    _check(torch_cuda, m, 8, seed=1)
+
+
+def test_spmm_matches_spmv_columns(native, torch_cuda):
+    """Column j of A X equals the SpMV of column j (within f64 rounding)."""
+    torch = torch_cuda
+    from diploma_research_gb300.generators import laplacian_3d_7pt
+
+    m = laplacian_3d_7pt(24)
+    A = csr5.from_csr(m)
+    rng = np.random.default_rng(3)
+    X = torch.tensor(rng.uniform(-1, 1, (m.dimensions.cols, 16)), device="cuda", dtype=torch.float64)
+    Y = torch.empty((m.dimensions.rows, 16), device="cuda", dtype=torch.float64)
+    spmm(A, X, Y)
+    for j in (0, 7, 15):
+        y = torch.empty(m.dimensions.rows, device="cuda", dtype=torch.float64)
+        A.spmv(X[:, j].contiguous(), y)
+        torch.cuda.synchronize()
+        assert torch.allclose(Y[:, j], y, rtol=0, atol=1e-13)
