@@ -455,6 +455,90 @@ def run_batch(args):
     return 0
 
 
+def run_adjoint(args):
+    """Differentiable-solve workload: 2-D anisotropic diffusion 1024^2 (5-point, kappa = exp(g), g a
+    Gaussian random field with length scale 16 cells, variance 1, seed 4, x:y anisotropy 10:1),
+    b = A x* (seed 4), loss L = ||x - x_t||^2 with x_t ~ U[-1,1].  Forward CG and adjoint CG
+    (lambda = A^{-T} dL/dx) to 1e-10 in FP64 and mixed precision, then dL/dA = -lambda x^T on the
+    pattern.  Gradients are checked by the adjoint identity on 16 random directions: lambda.db against
+    g.(A^{-1} db) and -lambda.(dA x) against g.(-A^{-1} dA x), the right-hand sides from FP64 forward
+    solves to 1e-12.  Prints one JSON line."""
+    import numpy as np
+    import torch
+
+    from diploma_research_gb300 import build as B
+
+    B.build()
+    from diploma_research_gb300.adjoint import cg_adjoint, spmv_transpose
+    from diploma_research_gb300.cg import CGSolver
+    from diploma_research_gb300.csr5 import csr5
+    from diploma_research_gb300.generators import WORKLOADS, rhs
+
+    w = WORKLOADS["aniso2d_1024"]
+    m = w["build"]()
+    n, nnz = m.dimensions.rows, m.nnz
+    xs, bh = rhs(m, w["seed"])
+    xt = np.random.default_rng(w["seed"] + 1).uniform(-1.0, 1.0, n)
+    A = csr5.from_csr(m)
+    stream = torch.cuda.current_stream()
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda", dtype=torch.float64)
+    b, xtd = dev(bh), dev(xt)
+    out = {"workload": f"aniso2d_1024: 2-D anisotropic diffusion 1024^2, n={n}, nnz={nnz}, CG to {TOL:g}"}
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    spmv_transpose(A, b, torch.empty_like(b), stream=stream)  # builds A^T once
+    torch.cuda.synchronize()
+    out["transpose_build_seconds"] = time.perf_counter() - t
+    tight = CGSolver(A, tol=1e-12, precision="fp64", stream=stream)
+    results = {}
+    for prec in ("fp64", "mixed"):
+        fwd = CGSolver(A, tol=TOL, precision=prec, stream=stream)
+        gv = torch.empty(nnz, device="cuda", dtype=torch.float64)
+        for rep in range(2):  # the first pass warms the graphs
+            x = torch.zeros(n, device="cuda", dtype=torch.float64)
+            lam = torch.zeros(n, device="cuda", dtype=torch.float64)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            _, rf = fwd.solve(b, x, stream=stream)
+            g = 2.0 * (x - xtd)
+            ra = cg_adjoint(A, g, x, lam, gv, tol=TOL, precision=prec, stream=stream)
+            torch.cuda.synchronize()
+            sec = time.perf_counter() - t0
+        results[prec] = (x, lam, gv)
+        out[prec] = {"seconds": sec, "forward_iterations": rf.iterations, "adjoint_iterations": ra.iterations,
+                     "forward_rel_residual": rf.rel_residual, "adjoint_rel_residual": ra.rel_residual,
+                     "forward_seconds_device": rf.seconds, "adjoint_seconds_device": ra.seconds}
+    # adjoint identity on random directions (FP64 forward solves to 1e-12 give the right-hand sides)
+    rng = np.random.default_rng(11)
+    Sd = m.to_scipy()
+    for prec in ("fp64", "mixed"):
+        x, lam, gv = results[prec]
+        g = 2.0 * (x - xtd)
+        xh = x.cpu().numpy()
+        ad, fd = [], []
+        for j in range(16):
+            if j % 2 == 0:
+                db = rng.standard_normal(n)
+                ad.append(float(lam @ dev(db)))
+                rhs_v = dev(db)
+            else:
+                dv = rng.standard_normal(nnz) * 0.1
+                dA = Sd.copy()
+                dA.data = dv
+                ad.append(float(gv @ dev(dv)))
+                rhs_v = dev(-(dA @ xh))
+            z = torch.zeros(n, device="cuda", dtype=torch.float64)
+            tight.solve(rhs_v, z, stream=stream)
+            fd.append(float(g @ z))
+        ad, fd = np.array(ad), np.array(fd)
+        out[prec]["adjoint_identity_rel_error"] = float(np.linalg.norm(ad - fd) / np.linalg.norm(fd))
+    lam64, lamx = results["fp64"][1], results["mixed"][1]
+    out["mixed_vs_fp64_lambda_rel_error"] = float(torch.linalg.norm(lamx - lam64) / torch.linalg.norm(lam64))
+    out["mixed_speedup"] = out["fp64"]["seconds"] / out["mixed"]["seconds"]
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -467,7 +551,10 @@ def main():
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven CG loop instead of the CUDA graph (profilers list every kernel)")
     ap.add_argument("--batch", default=None, help="comma-separated k: the multi-RHS block-CG workload")
+    ap.add_argument("--adjoint", action="store_true", help="the differentiable-solve workload (adjoint CG)")
     args = ap.parse_args()
+    if args.adjoint:
+        return run_adjoint(args)
     if args.batch:
         return run_batch(args)
     if args.spmv_only:

@@ -114,6 +114,10 @@ _SIGNATURES = {
     "dimgpu_block_cg_create": [_vp, _u32, ctypes.POINTER(cg_params), _vp, ctypes.POINTER(_vp)],
     "dimgpu_block_cg_destroy": [_vp],
     "dimgpu_block_cg_solve": [_vp, _vp, _u64, _vp, _u64, ctypes.POINTER(block_cg_stats), _vp, _vp, _vp],
+    "dimgpu_csr5_transpose": [_vp, _vp, ctypes.POINTER(_vp)],
+    "dimgpu_csr5_spmv_transpose": [_vp, _vp, _vp, _vp],
+    "dimgpu_csr5_pattern_outer": [_vp, _vp, _vp, _f64, _vp, _vp],
+    "dimgpu_cg_adjoint": [_vp, _vp, _vp, _vp, _vp, ctypes.POINTER(cg_params), ctypes.POINTER(cg_stats), _vp],
     "dimgpu_version": [],
 }
 

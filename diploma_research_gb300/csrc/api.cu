@@ -133,6 +133,8 @@ static void destroy_matrix(dimgpu_csr5* m) {
         spmm_scratch_release(static_cast<spmm_scratch*>(m->spmm_sc));
         delete static_cast<spmm_scratch*>(m->spmm_sc);
     }
+    if (m->transposed)
+        destroy_matrix(m->transposed);
     if (m->own_cal) {
         calibrator_release(m->own_cal);
         delete m->own_cal;

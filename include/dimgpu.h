@@ -208,6 +208,23 @@ DIMGPU_API int dimgpu_block_cg_solve(dimgpu_block_cg* s, const double* B, uint64
                                      dimgpu_block_cg_stats* stats, int64_t* col_iterations,
                                      double* col_rel_residual, void* stream);
 
+/* ---- differentiation (adjoint of x = A^{-1} b; no counterpart in the reference) ----------------- */
+
+/* A new handle holding A^T (deterministic: rows of A^T keep increasing column order). */
+DIMGPU_API int dimgpu_csr5_transpose(const dimgpu_csr5* m, void* stream, dimgpu_csr5** out);
+/* y := A^T x (x: rows, y: cols; device memory).  Builds A^T inside m on first use. */
+DIMGPU_API int dimgpu_csr5_spmv_transpose(const dimgpu_csr5* m, const double* x, double* y, void* stream);
+/* out[e] := scale * u[row(e)] * v[col(e)] for every stored element e, in the CSR order of the matrix
+ * given to dimgpu_csr5_from_csr (with scale = -1, u = lambda, v = x: dL/dA on the pattern). */
+DIMGPU_API int dimgpu_csr5_pattern_outer(const dimgpu_csr5* m, const double* u, const double* v, double scale,
+                                         double* out, void* stream);
+/* Adjoint CG: lambda := A^{-T} g by CG on A^T (lambda holds the initial guess on entry; dL/db = lambda),
+ * then grad_vals := -lambda x^T on the pattern (dL/dA, CSR order; grad_vals may be NULL).  Returns the
+ * solve status (DIMGPU_OK or _NOT_CONVERGED). */
+DIMGPU_API int dimgpu_cg_adjoint(const dimgpu_csr5* m, const double* g, const double* x, double* lambda,
+                                 double* grad_vals, const dimgpu_cg_params* params, dimgpu_cg_stats* stats,
+                                 void* stream);
+
 /* ---- diagnostics ------------------------------------------------------------------------------ */
 
 DIMGPU_API const char* dimgpu_last_error_string(void);
