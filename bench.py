@@ -33,6 +33,13 @@ sys.path.insert(0, ROOT)
 METRIC = "CG s to 1e-10 rel. residual, mixed vs FP64 on 1 GB300; SpMV GB/s vs HBM peak"
 WORKLOAD = "stencil27_128"
 TOL = 1e-10
+DESCR = {
+    "lap2d_512": "2-D 5-point Laplacian 512^2",
+    "stencil27_128": "3-D 27-point stencil 128^3",
+    "powerlaw_4m": "power-law rows (Zipf 2.0, up to 10,000 off-diagonals, symmetrised, diagonally dominant)",
+    "lap3d7_192": "3-D 7-point Laplacian 192^3",
+    "aniso2d_1024": "2-D anisotropic diffusion 1024^2 (kappa = exp(Gaussian random field), 10:1)",
+}
 
 
 def _peaks():
@@ -173,7 +180,7 @@ def run_reference(args):
     out = {"metric": METRIC, "value": value, "unit": "s", "impl": "reference", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(times) * 1e3,
            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": f"{WORKLOAD}: 3-D 27-point stencil 128^3, n={n}, nnz={m.nnz}, CG to {TOL:g}",
+           "config": {"workload": f"{WORKLOAD}: {DESCR[WORKLOAD]}, n={n}, nnz={m.nnz}, CG to {TOL:g}",
                       "global_batch": 1, "parallelism": "cpu-openmp"},
            "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -336,11 +343,12 @@ def run_gpu(args):
         out = {
             "metric": METRIC, "value": sec64, "unit": "s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": sec64 * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic (seeded 27-point stencil, b = A x*, x* ~ U[-1,1] seed 1)",
-            "config": {"workload": f"{WORKLOAD}: 3-D 27-point stencil 128^3, n={n}, nnz={nnz}, CG to {TOL:g} "
+            "dtype": "f64", "data": f"synthetic (seeded {WORKLOAD}, b = A x*, x* ~ U[-1,1])",
+            "config": {"workload": f"{WORKLOAD}: {DESCR[WORKLOAD]}, n={n}, nnz={nnz}, CG to {TOL:g} "
                                    "from x0 = 0, FP64", "global_batch": 1, "seq_len": n,
                        "parallelism": "replicas" if ws > 1 else "single-gpu",
-                       "l2": "inputs larger than L2 (702 MB of CSR5 data vs 129 MB L2); no flush"},
+                       "l2": f"inputs of {A.device_bytes / 1e6:.0f} MB of CSR5 data vs 129 MB L2"
+                             + ("; no flush" if A.device_bytes > 135e6 else "; L2-resident, no flush (solve-level timing)")},
             "iterations": res64.iterations, "rel_residual": res64.rel_residual, "rel_error_vs_xstar": err64,
             "mixed": {"value": secm, "unit": "s", "iterations": resm.iterations,
                       "reliable_updates": resm.reliable_updates, "rel_residual": resm.rel_residual,
@@ -349,7 +357,8 @@ def run_gpu(args):
                      "fp64_tflops": 2 * nnz / spmv_s / 1e12, "dot_fused_seconds": spmv_dot_s,
                      "f32_seconds": spmv32_s, "f32_gbps": (8 * nnz + 8 * n) / spmv32_s / 1e9},
             "roofline": {"bound": "hbm", "achieved": spmv_gbs, "peak": peak, "unit": "GB/s",
-                         "frac": spmv_gbs / peak, "traffic": _profile_traffic(), "kernel": "k_spmv<double,16>",
+                         "frac": spmv_gbs / peak,
+                         "traffic": _profile_traffic() if WORKLOAD == "stencil27_128" else None, "kernel": "k_spmv<double,16>",
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "fallback 6.8 TB/s"},
             "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
@@ -552,7 +561,12 @@ def main():
                     help="host-driven CG loop instead of the CUDA graph (profilers list every kernel)")
     ap.add_argument("--batch", default=None, help="comma-separated k: the multi-RHS block-CG workload")
     ap.add_argument("--adjoint", action="store_true", help="the differentiable-solve workload (adjoint CG)")
+    ap.add_argument("--workload", default=WORKLOAD, choices=sorted(DESCR),
+                    help="the system of the CG comparison (default: the 27-point 128^3 stencil)")
     args = ap.parse_args()
+    globals()["WORKLOAD"] = args.workload
+    globals()["TOL"] = __import__("diploma_research_gb300.generators", fromlist=["WORKLOADS"]).WORKLOADS[
+        args.workload]["tol"]
     if args.adjoint:
         return run_adjoint(args)
     if args.batch:
