@@ -48,7 +48,10 @@ class csr5_info(ctypes.Structure):
 
 class cg_params(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("max_it", ctypes.c_int64), ("precision", ctypes.c_int32),
-                ("use_graph", ctypes.c_int32), ("reliable_delta", ctypes.c_double)]
+                ("use_graph", ctypes.c_int32), ("reliable_delta", ctypes.c_double), ("engine", ctypes.c_int32)]
+
+
+CG_ENGINE_AUTO, CG_ENGINE_GRAPH, CG_ENGINE_FUSED = 0, 1, 2
 
 
 class cg_stats(ctypes.Structure):

@@ -29,16 +29,23 @@ class cg_result:
 
 
 _PREC = {"fp64": N.CG_FP64, "mixed": N.CG_MIXED}
+_ENGINE = {"auto": N.CG_ENGINE_AUTO, "graph": N.CG_ENGINE_GRAPH, "fused": N.CG_ENGINE_FUSED}
 
 
 class CGSolver:
+    """engine: "auto" (the library's choice, currently the graph), "graph" (one CUDA graph, three kernels
+    per iteration) or "fused" (one persistent cooperative kernel per solve); use_graph=False runs the
+    host-driven loop of kernels."""
+
     def __init__(self, A: csr5, tol: float = 1e-10, max_it: int = 100000, precision: str = "fp64",
-                 use_graph: bool = True, reliable_delta: float = 0.1, stream=None):
+                 use_graph: bool = True, reliable_delta: float = 0.1, stream=None, engine: str = "auto"):
         if precision not in _PREC:
             raise ValueError(f"precision must be one of {sorted(_PREC)}")
+        if engine not in _ENGINE:
+            raise ValueError(f"engine must be one of {sorted(_ENGINE)}")
         self.A = A
         self.params = N.cg_params(float(tol), int(max_it), _PREC[precision], 1 if use_graph else 0,
-                                  float(reliable_delta))
+                                  float(reliable_delta), _ENGINE[engine])
         h = ctypes.c_void_p()
         N.check(N.lib().dimgpu_cg_create(A._h, ctypes.byref(self.params), N.stream_ptr(stream), ctypes.byref(h)))
         self._h = h
@@ -74,9 +81,10 @@ class CGSolver:
 
 
 def cg(A: csr5, b, x0=None, tol: float = 1e-10, max_it: int = 100000, precision: str = "fp64",
-       use_graph: bool = True):
+       use_graph: bool = True, engine: str = "auto"):
     """One-shot solve: returns (x, cg_result)."""
-    return CGSolver(A, tol=tol, max_it=max_it, precision=precision, use_graph=use_graph).solve(b, x0)
+    return CGSolver(A, tol=tol, max_it=max_it, precision=precision, use_graph=use_graph,
+                    engine=engine).solve(b, x0)
 
 
 @dataclass
@@ -102,7 +110,7 @@ class BlockCGSolver:
             raise ValueError(f"precision must be one of {sorted(_PREC)}")
         self.A, self.k = A, int(k)
         self.params = N.cg_params(float(tol), int(max_it), _PREC[precision], 1 if use_graph else 0,
-                                  float(reliable_delta))
+                                  float(reliable_delta), N.CG_ENGINE_GRAPH)
         h = ctypes.c_void_p()
         N.check(N.lib().dimgpu_block_cg_create(A._h, self.k, ctypes.byref(self.params), N.stream_ptr(stream),
                                                ctypes.byref(h)))

@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "cg_common.cuh"
 #include "internal.hpp"
 
 namespace dimgpu {
@@ -37,23 +38,6 @@ namespace {
 
 constexpr int kVecThreads = 512;
 constexpr int kUnroll = 4;
-
-struct cg_state {
-    double rr;       // r.r of the current residual
-    double rr_new;   // r.r after this iteration's update
-    double alpha, beta;
-    double dot;      // s.As
-    double thresh2;  // (tol ||b||)^2
-    double bb;       // b.b
-    double maxrr;    // mixed: largest r.r since the last reliable update
-    double delta2;   // mixed: reliable_delta^2
-    double rr_true;  // last true residual r.r (f64)
-    int64_t iter, max_it, ru_count;
-    uint32_t stop;       // the solve has finished
-    uint32_t x_pending;  // f64: kernel C owes x += alpha s
-    uint32_t no_ru;      // mixed: no reliable update this iteration (guards its kernels)
-    uint32_t converged;
-};
 
 struct vec_ctx {
     cg_state* st;
@@ -470,6 +454,11 @@ struct dimgpu_cg_solver {
     uint32_t* counter = nullptr;
     double* norms = nullptr;
     dimgpu_calibrator cal{};  // SpMV scratch of this solver (f32 and f64 products take turns)
+    // persistent engine (cg_fused.cu)
+    int fused = 0, fgrid = 0;
+    uint32_t fwarps = 0;
+    double *f_cal_val = nullptr, *f_part = nullptr;
+    uint32_t *f_cal_row = nullptr, *f_flag = nullptr, *f_bar = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -491,7 +480,8 @@ void solver_free(dimgpu_cg_solver* s) {
     calibrator_release(&s->cal);
     for (void* p : {(void*)s->b, (void*)s->x, (void*)s->r, (void*)s->s, (void*)s->As, (void*)s->Ax, (void*)s->r32,
                     (void*)s->s32, (void*)s->As32, (void*)s->y32, (void*)s->st, (void*)s->part, (void*)s->counter,
-                    (void*)s->norms})
+                    (void*)s->norms, (void*)s->f_cal_val, (void*)s->f_part, (void*)s->f_cal_row, (void*)s->f_flag,
+                    (void*)s->f_bar})
         dev_free(p);
     delete s;
 }
@@ -666,6 +656,50 @@ int build_graph(dimgpu_cg_solver* s) {
     return DIMGPU_OK;
 }
 
+// One persistent kernel for the whole solve (needs s->x and s->b filled).
+int launch_fused(dimgpu_cg_solver* s, cudaStream_t st) {
+    const dimgpu_csr5* m = s->m;
+    cg_fused_args a{};
+    a.vals = m->vals;
+    a.vals32 = m->vals32;
+    a.col = m->col;
+    a.desc = reinterpret_cast<const uint32_t*>(m->tile_desc);
+    a.tile_ptr = m->tile_ptr;
+    a.tdo_ptr = m->tdo_ptr;
+    a.tdo = m->tdo;
+    a.row_ptr = m->row_ptr;
+    a.T = m->tile_count;
+    a.rows = m->rows;
+    a.tail_start = m->tail_start;
+    a.nwarps = s->fwarps;
+    a.tpw = a.T ? (a.T + a.nwarps - 1) / a.nwarps : 0;
+    a.tail_warp = a.T ? (uint32_t)((a.T - 1) / a.tpw) : 0u;
+    a.b = s->b;
+    a.x = s->x;
+    a.r = s->r;
+    a.s = s->s;
+    a.As = s->As;
+    a.Ax = s->Ax;
+    a.r32 = s->r32;
+    a.s32 = s->s32;
+    a.As32 = s->As32;
+    a.y32 = s->y32;
+    a.cal_val = s->f_cal_val;
+    a.cal_row = s->f_cal_row;
+    a.flag = s->f_flag;
+    a.part = s->f_part;
+    a.bar = s->f_bar;
+    a.status = s->cal.status;
+    a.st = s->st;
+    a.tol2 = s->params.tol * s->params.tol;
+    a.delta2 = s->params.reliable_delta * s->params.reliable_delta;
+    a.max_it = s->params.max_it;
+    a.mixed = mixed(s) ? 1 : 0;
+    a.grid = s->fgrid;
+    DG_CUDA(cudaMemsetAsync(s->f_bar, 0, 64 * sizeof(uint32_t), st));
+    return launch_cg_fused(a, st);
+}
+
 }  // namespace
 
 extern "C" {
@@ -721,7 +755,24 @@ int dimgpu_cg_create(const dimgpu_csr5* m, const dimgpu_cg_params* params, void*
             rc = cuda_fail(cudaGetLastError(), "cudaEventCreate");
             break;
         }
-        if (params->use_graph && (rc = build_graph(s)) != DIMGPU_OK) break;
+        if (params->use_graph && params->engine == DIMGPU_CG_ENGINE_FUSED) {
+            int g = 0;
+            const int frc = cg_fused_grid(m, &g);
+            if (frc == DIMGPU_OK) {
+                s->fused = 1;
+                s->fgrid = g;
+                s->fwarps = cg_fused_warps(g);
+                if ((rc = dev_alloc_n(&s->f_cal_val, s->fwarps)) != DIMGPU_OK) break;
+                if ((rc = dev_alloc_n(&s->f_cal_row, s->fwarps)) != DIMGPU_OK) break;
+                if ((rc = dev_alloc_n(&s->f_flag, s->fwarps)) != DIMGPU_OK) break;
+                if ((rc = dev_alloc_n(&s->f_part, 6 * (uint64_t)g)) != DIMGPU_OK) break;
+                if ((rc = dev_alloc_n(&s->f_bar, 64)) != DIMGPU_OK) break;
+            } else if (params->engine == DIMGPU_CG_ENGINE_FUSED) {
+                rc = frc;
+                break;
+            }
+        }
+        if (params->use_graph && !s->fused && (rc = build_graph(s)) != DIMGPU_OK) break;
     } while (false);
     if (rc != DIMGPU_OK) {
         solver_free(s);
@@ -750,7 +801,9 @@ int dimgpu_cg_solve(dimgpu_cg_solver* s, const double* b, double* x, dimgpu_cg_s
     DG_CUDA(cudaMemcpyAsync(s->st, &init, sizeof(init), cudaMemcpyHostToDevice, st));
     DG_CUDA(cudaMemsetAsync(s->cal.status, 0, sizeof(uint32_t), st));
     DG_CUDA(cudaEventRecord(s->ev0, st));
-    if (s->exec) {
+    if (s->fused) {
+        DG_CHECK(launch_fused(s, st));
+    } else if (s->exec) {
         DG_CUDA(cudaGraphLaunch(s->exec, st));
     } else {
         const vec_ctx c = make_ctx(s);

@@ -53,10 +53,11 @@ struct spmv_plan {
 struct dimgpu_calibrator {
     int device = 0;
     uint32_t nslots = 0;
-    double* cal_val = nullptr;    // [nslots] head partial sum of each warp's first row
-    uint32_t* cal_row = nullptr;  // [nslots] that row, MSB set when the slot is valid
-    double* dot_part = nullptr;   // [nslots + 1] per-warp partials of the fused dot product
-    uint32_t* counter = nullptr;  // CTA completion ticket (reset by the last CTA)
+    double* cal_val = nullptr;    // [nslots] row fragment each warp run publishes for a later run
+    uint32_t* cal_row = nullptr;  // [nslots] that fragment's row
+    uint32_t* flag = nullptr;     // [nslots] (launch epoch << 2) | fragment kind of each run
+    double* dot_part = nullptr;   // [nslots + 1] per-CTA partials of the fused dot product
+    uint32_t* counter = nullptr;  // [4] completion ticket, -, run counter, launch epoch
     uint32_t* status = nullptr;   // device status word (dimgpu::device_status)
 };
 

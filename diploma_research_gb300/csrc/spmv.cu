@@ -24,11 +24,17 @@
 //     columns without a row start needs;
 //   * the head segment of the tile and the segment running off its end feed an in-order carry
 //     chain inside the warp, so rows crossing tile boundaries are summed left to right.
-// Calibrator (csr5.h:526-538, 750-754).  A warp's first row, when it started before the warp's
-// first tile, is not written: its partial sum goes to the warp's calibrator slot.  The last CTA to
-// finish (completion ticket) adds the slots to y in warp order, then computes the CSR tail
-// (csr5.h:756-782) and, optionally, the fused dot x.y and alpha = rr / (x.y) for CG.  y is fully
-// overwritten: empty rows below the tail are zeroed from the list built at conversion.
+// Calibrator (csr5.h:526-538, 750-754) as a decoupled look-back.  CTAs take consecutive run numbers
+// in the order they start (one atomic per CTA), each warp owning run number cta * WPC + warp.  A row
+// that crosses runs is finished by the run holding its last element: when a run ends, it publishes
+// the fragment a later run needs (its open row's partial sum, or -- when no row starts in the whole
+// run -- the run's sum of the row passing through) under a flag word tagged with the launch epoch;
+// the finishing run looks back over the flags of earlier runs (bounded waits; earlier runs have always
+// started, so no wait depends on residency) and adds the fragments in run order, left to right as the
+// reference's serial calibrator pass does.  The last CTA to finish (completion ticket) computes the
+// CSR tail (csr5.h:756-782) and, optionally, the fused dot x.y (per-CTA partials, fixed order) and
+// alpha = rr / (x.y) for CG.  y is fully overwritten: empty rows below the tail are zeroed from the
+// list built at conversion.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -37,18 +43,10 @@
 #include "common.cuh"
 #include "internal.hpp"
 #include "layout.cuh"
+#include "spmv_tile.cuh"
 
 namespace dimgpu {
 namespace {
-
-template <int SIGMA>
-struct word_of {
-    using type = uint32_t;
-};
-template <>
-struct word_of<32> {
-    using type = uint64_t;
-};
 
 template <typename VT>
 struct spmv_params {
@@ -68,10 +66,11 @@ struct spmv_params {
     uint32_t nwarps;
     const uint32_t* empty_rows;
     uint32_t n_empty;
-    double* cal_val;
-    uint32_t* cal_row;
-    double* dot_part;
-    uint32_t* counter;
+    double* frag_val;    // [nwarps] fragment a run publishes for a later run
+    uint32_t* frag_row;  // [nwarps] its row
+    uint32_t* flag;      // [nwarps] (epoch << 2) | fragment kind, release-stored after the fragment
+    double* cta_part;    // [grid] per-CTA partials of the fused dot
+    uint32_t* words;     // [0] completion ticket, [2] run counter, [3] launch epoch
     uint32_t* status;
     double* dot_out;
     const double* rr;
@@ -79,52 +78,59 @@ struct spmv_params {
     uint32_t* halt;
 };
 
-template <typename VT, int SIGMA>
-struct tile_geom {
-    using Word = typename word_of<SIGMA>::type;
-    static constexpr uint32_t TS = SIGMA * 32;
-    static constexpr uint32_t VBYTES = TS * sizeof(VT);
-    static constexpr uint32_t CBYTES = TS * 4;
-    static constexpr uint32_t DBYTES = 32 * sizeof(Word);
-    static constexpr uint32_t STAGE = VBYTES + CBYTES + DBYTES;
-    static constexpr desc_fields F = fields_for(SIGMA, 32);
-    static constexpr uint64_t YMASK = (1ull << F.yb) - 1;
-    static constexpr uint64_t FMASK = (SIGMA == 64) ? ~0ull : ((1ull << SIGMA) - 1);
-};
+constexpr uint32_t kFragNone = 0, kFragCarry = 1, kFragThrough = 2;
 
-// Loads lane `lane`'s column (SIGMA values and column indices) from a shared stage.
-template <typename VT, int SIGMA>
-__device__ __forceinline__ void load_column(const unsigned char* stage, unsigned lane, VT (&v)[SIGMA],
-                                            uint32_t (&ci)[SIGMA]) {
-    using G = tile_geom<VT, SIGMA>;
-    const uint4* sc = reinterpret_cast<const uint4*>(stage + G::VBYTES);
-#pragma unroll
-    for (int j = 0; j < SIGMA / 4; ++j) {
-        const uint4 q = sc[j * 32 + lane];
-        ci[4 * j + 0] = q.x;
-        ci[4 * j + 1] = q.y;
-        ci[4 * j + 2] = q.z;
-        ci[4 * j + 3] = q.w;
-    }
-    if constexpr (sizeof(VT) == 8) {
-        const double2* sv = reinterpret_cast<const double2*>(stage);
-#pragma unroll
-        for (int j = 0; j < SIGMA / 2; ++j) {
-            const double2 d = sv[j * 32 + lane];
-            v[2 * j + 0] = d.x;
-            v[2 * j + 1] = d.y;
-        }
-    } else {
-        const float4* sv = reinterpret_cast<const float4*>(stage);
-#pragma unroll
-        for (int j = 0; j < SIGMA / 4; ++j) {
-            const float4 d = sv[j * 32 + lane];
-            v[4 * j + 0] = d.x;
-            v[4 * j + 1] = d.y;
-            v[4 * j + 2] = d.z;
-            v[4 * j + 3] = d.w;
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Bounded wait for run k's flag of this launch; returns its fragment kind, or kFragNone after recording
+// kStatusWaitTimeout.  Polls without acquire (no cache invalidation per poll), then one acquire.
+__device__ __forceinline__ uint32_t wait_run(const uint32_t* flag, uint32_t epoch, uint32_t* status) {
+    if ((ld_relaxed_u32(flag) >> 2) != epoch) {
+        const uint64_t t0 = global_ns();
+        while ((ld_relaxed_u32(flag) >> 2) != epoch) {
+            if (global_ns() - t0 > DIMGPU_WAIT_NS) {
+                record_status(status, kStatusWaitTimeout);
+                return kFragNone;
+            }
         }
     }
+    return ld_acquire_u32(flag) & 3u;
+}
+
+// Final value of row R, whose last fragment `own` this caller holds: the runs before `run` that hold
+// R's earlier fragments are found by looking back (through-fragments, then the run where R started,
+// which published its carry); the fragments are then added in run order, as a serial left-to-right
+// pass over the runs would.  Runs are numbered in launch order, so every run waited on has started.
+template <typename VT>
+__device__ VT close_row(const spmv_params<VT>& p, uint32_t run, uint32_t R, VT own, uint32_t epoch) {
+    uint32_t i = run;
+    while (i > 0) {
+        --i;
+        const uint32_t kind = wait_run(&p.flag[i], epoch, p.status);
+        const uint32_t fr = __ldcg(&p.frag_row[i]);
+        if (fr != R || kind == kFragNone) {
+            record_status(p.status, kStatusBadIndex);  // no earlier fragment of R: the format is inconsistent
+            return own;
+        }
+        if (kind == kFragCarry)
+            break;
+    }
+    VT acc = (VT)__ldcg(&p.frag_val[i]);
+    for (uint32_t k = i + 1; k < run; ++k)
+        acc += (VT)__ldcg(&p.frag_val[k]);
+    return acc + own;
 }
 
 template <typename VT, int SIGMA, int WPC, int STAGES, bool DOT>
@@ -132,14 +138,18 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
     using G = tile_geom<VT, SIGMA>;
     using Word = typename G::Word;
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ uint32_t s_last;
+    __shared__ uint32_t s_last, s_cta, s_epoch;
     __shared__ double s_red[WPC];
 
     if (p.halt && *reinterpret_cast<volatile const uint32_t*>(p.halt))
         return;  // a previous stage of a CG iteration has already stopped the solve
 
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const uint32_t gw = blockIdx.x * WPC + warp;
+    // CTAs take run numbers in the order they start, so a run only ever waits for runs already running
+    if (threadIdx.x == 0) {
+        s_cta = atomicAdd(&p.words[2], 1u);
+        s_epoch = *reinterpret_cast<volatile const uint32_t*>(&p.words[3]) + 1u;
+    }
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem) + warp * STAGES;
     unsigned char* ring = smem + 128 * ((WPC * STAGES * 8 + 127) / 128) + (size_t)warp * STAGES * G::STAGE;
 
@@ -147,27 +157,21 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < p.n_empty;
          i += (uint64_t)gridDim.x * blockDim.x)
         p.y[p.empty_rows[i]] = VT(0);
+    __syncthreads();
+    const uint32_t cta = s_cta;
+    const uint32_t epoch = (s_epoch & 0x3fffffffu) ? (s_epoch & 0x3fffffffu) : 1u;  // flags start at epoch 0
+    const uint32_t run = cta * WPC + warp;
 
-    const uint64_t t_begin = min(p.T, (uint64_t)gw * p.tpw);
+    const uint64_t t_begin = min(p.T, (uint64_t)run * p.tpw);
     const uint64_t t_end = min(p.T, t_begin + p.tpw);
 
-    double dot_acc = 0.0;
-    bool open = false, cal_valid = false;
-    VT carry = VT(0), cal = VT(0);
-    uint32_t carry_row = 0, cal_row = 0;
-
-    auto write_row_lane0 = [&](uint32_t row, VT val) {
-        if (lane == 0) {
-            p.y[row] = val;
-            if constexpr (DOT)
-                dot_acc += (double)val * (double)ldg_keep(p.x + row);
-        }
-    };
+    warp_chain<VT> ch;
+    const tile_io<VT> io{p.x, p.y, p.tdo_ptr, p.tdo, p.rows};
+    const uint64_t pol_keep = policy_evict_last();
 
     if (t_begin < t_end) {
         const Word* gdesc = reinterpret_cast<const Word*>(p.desc);
         const uint64_t pol = policy_evict_first();
-        const uint64_t pol_keep = policy_evict_last();
         if (lane == 0) {
             for (int s = 0; s < STAGES; ++s)
                 mbar_init(&bars[s], 1);
@@ -194,159 +198,14 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
             const int s = (int)(i % STAGES);
             const uint32_t par = (uint32_t)((i / STAGES) & 1);
             const uint32_t raw = raw_cur;
-            const uint32_t row_stop = raw_next & ~kDirty;
-            const uint32_t row_start = raw & ~kDirty;
+            const uint32_t raw_n = raw_next;
             raw_cur = raw_next;
             raw_next = (t + 2 <= p.T) ? __ldg(&p.tile_ptr[t + 2]) : 0u;
             if (!mbar_wait_bounded(&bars[s], par, p.status)) {
                 failed = true;
                 break;
             }
-            unsigned char* st = ring + (size_t)s * G::STAGE;
-            const Word* sd = reinterpret_cast<const Word*>(st + G::VBYTES + G::CBYTES);
-
-            VT v[SIGMA];
-            uint32_t ci[SIGMA];
-            load_column<VT, SIGMA>(st, lane, v, ci);
-            const Word w = sd[lane];
-            VT xv[SIGMA];
-#pragma unroll
-            for (int r = 0; r < SIGMA; ++r)
-                xv[r] = ldg_x(p.x + ci[r], pol_keep);
-            // the fused dot needs x at this tile's rows: fetch them now, off the write-out's path
-            VT xrow = VT(0);
-            if constexpr (DOT) {
-                if (row_start + lane < p.rows)
-                    xrow = ldg_x(p.x + row_start + lane, pol_keep);
-            }
-            const uint32_t flag = (uint32_t)((uint64_t(w) >> (G::F.yb + G::F.sb)) & G::FMASK);
-            const bool capped = (__shfl_sync(kFull, flag, 0) & 1u) != 0;
-            // Every lane now holds its column: the value area of the stage becomes the staging
-            // buffer of this tile's segment sums (slot = segment index, at most sigma*32 of them).
-            __syncwarp();
-            VT* ystage = reinterpret_cast<VT*>(st);
-            const bool dirty = (raw & kDirty) != 0;
-            const uint32_t optr = dirty ? __ldg(&p.tdo_ptr[t]) : 0u;
-            auto row_of = [&](uint32_t idx) -> uint32_t {
-                return row_start + (dirty ? __ldg(&p.tdo[optr + idx]) : idx);
-            };
-
-            VT H, Lt;
-            uint32_t K, row_last;
-            if (raw == row_stop) {
-                // partition_fast_track (csr5.h:562-574): the whole tile is one row
-                VT acc = VT(0);
-#pragma unroll
-                for (int r = 0; r < SIGMA; ++r)
-                    acc = fma(v[r], xv[r], acc);
-                H = warp_sum(acc);
-                Lt = H;
-                K = 1;
-                row_last = row_start;
-            } else {
-                const uint32_t yoff = (uint32_t)(uint64_t(w) & G::YMASK);
-                const uint32_t fl = flag | (lane == 0 ? 1u : 0u);
-                const uint32_t present = __ballot_sync(kFull, fl != 0);
-
-                // Segments of this column: segment yoff + k is staged at slot[k].  Branch-free: a
-                // row start closes the open segment (predicated store) and restarts the sum.
-                VT* slot = ystage + yoff;
-                VT sum = VT(0), red = VT(0);
-                uint32_t k = 0;
-                bool seen = false;
-#pragma unroll
-                for (int r = 0; r < SIGMA; ++r) {
-                    const bool bit = ((fl >> r) & 1u) != 0;
-                    const bool close = bit && seen;
-                    if (close)
-                        slot[k] = sum;
-                    k += close ? 1u : 0u;
-                    red = (bit && !seen) ? sum : red;
-                    seen = seen || bit;
-                    sum = bit ? VT(0) : sum;
-                    sum = fma(v[r], xv[r], sum);
-                }
-                const VT L = seen ? sum : VT(0);
-                red = seen ? red : sum;
-
-                // segmented suffix sums of the red parts, terminated by columns with a row start
-                VT U = red;
-                uint32_t stopped = (present >> lane) & 1u;
-                const int steps = scan_steps_for(present);
-                for (int q = 0, d = 1; q < steps; ++q, d <<= 1) {
-                    const VT u2 = __shfl_down_sync(kFull, U, d);
-                    const uint32_t s2 = __shfl_down_sync(kFull, stopped, d);
-                    if (!stopped && lane + d < 32) {
-                        U += u2;
-                        stopped |= s2;
-                    }
-                }
-                const VT nxt = __shfl_down_sync(kFull, U, 1);
-                const VT seg_total = L + (lane == 31 ? VT(0) : nxt);
-                const uint32_t last_lane = 31u - __clz(present);
-                const bool is_present = ((present >> lane) & 1u) != 0;
-                if (is_present && lane != last_lane)
-                    slot[k] = seg_total;  // the column's open segment, closed by a later column
-                uint32_t my_row_last = 0;
-                if (lane == last_lane)
-                    my_row_last = row_of(yoff + k);
-                K = __shfl_sync(kFull, yoff + k + 1, last_lane);
-                Lt = __shfl_sync(kFull, seg_total, last_lane);
-                row_last = __shfl_sync(kFull, my_row_last, last_lane);
-                __syncwarp();
-                H = (K == 1) ? Lt : ystage[0];  // segment 0 sits in slot 0 whenever it closed in this tile
-            }
-
-            // in-order carry chain over the warp's tiles (uniform across lanes)
-            bool head_staged = false;
-            if (K == 1) {
-                if (capped) {
-                    if (open)
-                        write_row_lane0(carry_row, carry);
-                    open = true;
-                    carry = H;
-                    carry_row = row_start;
-                } else if (open) {
-                    carry += H;
-                } else {
-                    cal += H;
-                    cal_row = row_start;
-                    cal_valid = true;
-                }
-            } else {
-                if (capped || open) {
-                    if (capped && open)
-                        write_row_lane0(carry_row, carry);
-                    if (!capped && lane == 0)
-                        ystage[0] = carry + H;  // the row that began before this tile closes here
-                    head_staged = true;
-                } else {
-                    cal += H;
-                    cal_row = row_start;
-                    cal_valid = true;
-                }
-                open = true;
-                carry = Lt;
-                carry_row = row_last;
-            }
-            // write the tile's closed rows coalesced (slots 0 or 1 .. K-2; slot K-1 is the carry)
-            __syncwarp();
-            if (K > 1) {
-                const uint32_t lo = head_staged ? 0u : 1u;
-                VT xfirst = VT(0);
-                if constexpr (DOT)
-                    xfirst = __shfl_down_sync(kFull, xrow, lo);  // x[row_start + lo + lane]
-                for (uint32_t j = lo + lane; j + 1 < K; j += 32) {
-                    const VT val = ystage[j];
-                    const uint32_t row = row_of(j);
-                    st_keep(p.y + row, val, pol_keep);
-                    if constexpr (DOT) {
-                        const bool have = !dirty && j == lo + lane && lane + lo < 32;
-                        const VT xr = have ? xfirst : ldg_x(p.x + row, pol_keep);
-                        dot_acc = fma((double)val, (double)xr, dot_acc);
-                    }
-                }
-            }
+            process_tile<VT, SIGMA, DOT>(io, ring + (size_t)s * G::STAGE, lane, t, raw, raw_n, pol_keep, ch);
 
             __syncwarp();
             if (lane == 0 && t + STAGES < t_end) {
@@ -360,25 +219,58 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
                 const uint64_t i2 = t2 - t_begin;
                 (void)mbar_wait_bounded(&bars[i2 % STAGES], (uint32_t)((i2 / STAGES) & 1), p.status);
             }
-        } else if (open) {
-            write_row_lane0(carry_row, carry);
+        }
+
+        // Does the row open at the end of this run go on after it?  Yes unless the next tile begins
+        // with a row start (or, after the last tile, unless the CSR tail begins with a fresh row).
+        bool cont_after;
+        if (t_end < p.T) {
+            const uint64_t w0 = (uint64_t)__ldg(&gdesc[t_end * 32]);
+            cont_after = ((w0 >> (G::F.yb + G::F.sb)) & 1u) == 0;
+        } else {
+            cont_after = p.tail_start < p.rows && (uint64_t)p.row_ptr[p.tail_start] != p.T * G::TS;
+        }
+        const bool through = ch.cal_valid && !ch.open;
+        if (lane == 0) {
+            // publish the fragment a later run needs (the flag word is written for every run)
+            uint32_t kind = kFragNone;
+            if (ch.open && cont_after) {
+                p.frag_val[run] = (double)ch.carry;
+                p.frag_row[run] = ch.carry_row;
+                kind = kFragCarry;
+            } else if (through && cont_after) {
+                p.frag_val[run] = (double)ch.cal;
+                p.frag_row[run] = ch.cal_row;
+                kind = kFragThrough;
+            }
+            st_release_u32(&p.flag[run], (epoch << 2) | kind);
+            // rows this run finishes: its open row when it ends here, and the row it began inside
+            if (ch.open && !cont_after)
+                chain_write_row<VT, DOT>(io, ch, 0, ch.carry_row, ch.carry);
+            if (ch.cal_valid && (!through || !cont_after)) {
+                const VT v = close_row<VT>(p, run, ch.cal_row, ch.cal, epoch);
+                chain_write_row<VT, DOT>(io, ch, 0, ch.cal_row, v);
+            }
         }
     }
-    if (lane == 0) {
-        p.cal_val[gw] = (double)cal;
-        p.cal_row[gw] = cal_valid ? (cal_row | kDirty) : 0u;
-    }
+    // per-CTA partial of the fused dot, in warp order
     if constexpr (DOT) {
-        const double d = warp_sum(dot_acc);
+        const double d = warp_sum(ch.dot_acc);
         if (lane == 0)
-            p.dot_part[gw] = d;
+            s_red[warp] = d;
     }
 
-    // ---- completion ticket; the last CTA resolves calibrators, the tail and the epilogue ----
-    __threadfence();
+    // ---- completion ticket; the last CTA computes the CSR tail and the epilogue ----
     __syncthreads();
     if (threadIdx.x == 0) {
-        const uint32_t ticket = atomicAdd(p.counter, 1u);
+        if constexpr (DOT) {
+            double d = 0.0;
+            for (int w = 0; w < WPC; ++w)
+                d += s_red[w];
+            p.cta_part[cta] = d;
+        }
+        __threadfence();
+        const uint32_t ticket = atomicAdd(&p.words[0], 1u);
         s_last = (ticket == gridDim.x - 1) ? 1u : 0u;
     }
     __syncthreads();
@@ -386,48 +278,30 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
         return;
     __threadfence();
 
+    // CSR tail (csr5.h:756-782): one row per thread; a first row that began inside the tiles is closed
+    // by looking back over the runs like any other row.
     double fix_dot = 0.0;
-    for (uint32_t wi = threadIdx.x; wi < p.nwarps; wi += blockDim.x) {
-        const uint32_t cr = __ldcg(&p.cal_row[wi]);
-        if (!(cr & kDirty))
-            continue;
-        if (wi > 0 && __ldcg(&p.cal_row[wi - 1]) == cr)
-            continue;  // not the first slot of this row
-        const uint32_t R = cr & ~kDirty;
-        VT acc = __ldcg(&p.y[R]);
-        double added = 0.0;
-        for (uint32_t w2 = wi; w2 < p.nwarps; ++w2) {
-            if (__ldcg(&p.cal_row[w2]) != cr)
-                break;
-            const VT c = (VT)__ldcg(&p.cal_val[w2]);
-            acc += c;
-            added += (double)c;
-        }
-        p.y[R] = acc;
-        if constexpr (DOT)
-            fix_dot += added * (double)p.x[R];
-    }
-    __syncthreads();
     const uint64_t first_tail = p.T * G::TS;
+    const uint32_t nruns = p.T ? (uint32_t)((p.T + p.tpw - 1) / p.tpw) : 0u;
     for (uint64_t r = (uint64_t)p.tail_start + threadIdx.x; r < p.rows; r += blockDim.x) {
-        const uint64_t s = (r == p.tail_start) ? first_tail : (uint64_t)p.row_ptr[r];
+        const uint64_t s0 = (r == p.tail_start) ? first_tail : (uint64_t)p.row_ptr[r];
         const uint64_t e = p.row_ptr[r + 1];
         VT acc = VT(0);
-        for (uint64_t k = s; k < e; ++k)
+        for (uint64_t k = s0; k < e; ++k)
             acc = fma(p.vals[k], p.x[p.col[k]], acc);
-        if (r == p.tail_start && (uint64_t)p.row_ptr[r] != first_tail)
-            p.y[r] = __ldcg(&p.y[r]) + acc;
-        else
-            p.y[r] = acc;
+        if (r == p.tail_start && (uint64_t)p.row_ptr[r] != first_tail && nruns > 0)
+            acc = close_row<VT>(p, nruns, (uint32_t)r, acc, epoch);
+        p.y[r] = acc;
         if constexpr (DOT)
             fix_dot += (double)acc * (double)p.x[r];
     }
     if constexpr (DOT) {
         double part = fix_dot;
-        for (uint32_t wi = threadIdx.x; wi < p.nwarps; wi += blockDim.x)
-            part += __ldcg(&p.dot_part[wi]);
-        // warp sums, then the WPC warp sums in order (any block size; fixed order)
+        for (uint32_t c = threadIdx.x; c < gridDim.x; c += blockDim.x)
+            part += __ldcg(&p.cta_part[c]);
+        // warp sums, then the WPC warp sums in order (fixed order)
         part = warp_sum(part);
+        __syncthreads();
         if (lane == 0)
             s_red[warp] = part;
         __syncthreads();
@@ -450,8 +324,11 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
             }
         }
     }
-    if (threadIdx.x == 0)
-        *p.counter = 0u;
+    if (threadIdx.x == 0) {
+        p.words[0] = 0u;
+        p.words[2] = 0u;
+        p.words[3] = epoch;
+    }
 }
 
 template <typename VT, int SIGMA, int WPC, int STAGES>
@@ -485,10 +362,11 @@ int launch_cfg(const dimgpu_csr5* m, const VT* vals, const VT* x, VT* y, dimgpu_
     p.nwarps = pl.nwarps;
     p.empty_rows = m->empty_rows;
     p.n_empty = m->n_empty;
-    p.cal_val = cal->cal_val;
-    p.cal_row = cal->cal_row;
-    p.dot_part = cal->dot_part;
-    p.counter = cal->counter;
+    p.frag_val = cal->cal_val;
+    p.frag_row = cal->cal_row;
+    p.flag = cal->flag;
+    p.cta_part = cal->dot_part;
+    p.words = cal->counter;
     p.status = cal->status;
     p.dot_out = ep.dot_out;
     p.rr = ep.rr;
@@ -557,6 +435,8 @@ int calibrator_init(dimgpu_calibrator* c, const dimgpu_csr5* m) {
     DG_CHECK(dev_alloc_n(&c->cal_val, c->nslots));
     DG_CHECK(dev_alloc_n(&c->cal_row, c->nslots));
     DG_CHECK(dev_alloc_n(&c->dot_part, c->nslots + 1));
+    DG_CHECK(dev_alloc_n(&c->flag, c->nslots));
+    DG_CUDA(cudaMemset(c->flag, 0, sizeof(uint32_t) * c->nslots));
     DG_CHECK(dev_alloc_n(&c->counter, 4));
     DG_CHECK(dev_alloc_n(&c->status, 4));
     DG_CUDA(cudaMemset(c->counter, 0, 16));
@@ -568,6 +448,7 @@ void calibrator_release(dimgpu_calibrator* c) {
     dev_free(c->cal_val);
     dev_free(c->cal_row);
     dev_free(c->dot_part);
+    dev_free(c->flag);
     dev_free(c->counter);
     dev_free(c->status);
     c->cal_val = nullptr;
@@ -636,10 +517,12 @@ constexpr uint32_t kStaticSlots = 4096;  // warp slots: enough for 256 SMs x 16 
 constexpr size_t kStaticValBytes = 8 * kStaticSlots;
 constexpr size_t kStaticDotBytes = 8 * (kStaticSlots + 32);
 constexpr size_t kStaticRowBytes = 4 * kStaticSlots;
-constexpr size_t kStaticWordBytes = 256;  // completion ticket + status word, own 256-byte block
-constexpr size_t kStaticScratchBytes = kStaticValBytes + kStaticDotBytes + kStaticRowBytes + kStaticWordBytes;
+constexpr size_t kStaticFlagBytes = 4 * kStaticSlots;
+constexpr size_t kStaticWordBytes = 256;  // ticket, status, run counter, epoch: own 256-byte block
+constexpr size_t kStaticScratchBytes =
+    kStaticValBytes + kStaticDotBytes + kStaticRowBytes + kStaticFlagBytes + kStaticWordBytes;
 
-// 82,432 bytes of device memory, shared by every call of dimgpu_csr5_spmv_static_scratch on a device.
+// 98,816 bytes of device memory, shared by every call of dimgpu_csr5_spmv_static_scratch on a device.
 static __device__ __align__(256) unsigned char g_spmv_static_scratch[kStaticScratchBytes];
 
 constexpr int kMaxDevices = 64;
@@ -688,11 +571,14 @@ extern "C" int dimgpu_csr5_spmv_static_scratch(const dimgpu_csr5* m, const doubl
     cal.cal_val = reinterpret_cast<double*>(base);
     cal.dot_part = reinterpret_cast<double*>(base + kStaticValBytes);
     cal.cal_row = reinterpret_cast<uint32_t*>(base + kStaticValBytes + kStaticDotBytes);
-    cal.counter = reinterpret_cast<uint32_t*>(base + kStaticValBytes + kStaticDotBytes + kStaticRowBytes);
+    cal.flag = reinterpret_cast<uint32_t*>(base + kStaticValBytes + kStaticDotBytes + kStaticRowBytes);
+    cal.counter = reinterpret_cast<uint32_t*>(base + kStaticValBytes + kStaticDotBytes + kStaticRowBytes +
+                                              kStaticFlagBytes);
     cal.status = cal.counter + 1;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    // The array keeps whatever the previous call left; the completion ticket and the status word must
-    // start at zero.  (The slots themselves are written by every warp before they are read.)
-    DG_CUDA(cudaMemsetAsync(cal.counter, 0, 2 * sizeof(uint32_t), s));
+    // The array keeps whatever the previous call left; the completion ticket, the status word and the run
+    // counter must start at zero.  The launch epoch (word 3) carries over: the flags of earlier calls
+    // hold older epochs, and a zero-initialised array starts at epoch 0, which no launch uses.
+    DG_CUDA(cudaMemsetAsync(cal.counter, 0, 3 * sizeof(uint32_t), s));
     return launch_spmv_f64(m, x, y, &cal, spmv_epilogue{}, s);
 }

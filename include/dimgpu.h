@@ -117,7 +117,7 @@ DIMGPU_API int dimgpu_csr5_spmv_host(const dimgpu_csr5* m, const double* x_host,
 DIMGPU_API int dimgpu_csr5_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calibrator* cal, void* stream);
 
 /* y := A x like dimgpu_csr5_spmv, but neither this call nor the library allocates anything: the
- * scratch (per-warp row fragments, completion ticket, status word) is a fixed array of 82,432 bytes
+ * scratch (per-warp row fragments, completion ticket, status word) is a fixed array of 98,816 bytes
  * compiled into the library, present on every GPU that loads it until the process exits.  It has no
  * counterpart in the reference; it exists for callers that cannot allocate device memory when they
  * multiply (a plugin whose host reserved all device memory, a latency-bound loop that cannot afford
@@ -162,9 +162,14 @@ typedef struct {
     double tol;        /* stop when ||r|| <= tol * ||b|| */
     int64_t max_it;    /* iteration cap */
     int32_t precision; /* DIMGPU_CG_FP64 or DIMGPU_CG_MIXED */
-    int32_t use_graph; /* 1: whole solve as one CUDA graph with a device-side while loop */
+    int32_t use_graph; /* 0: host-driven loop of kernels; otherwise the engine below */
     double reliable_delta; /* mixed only: replace the residual when it dropped by this factor; 0 = 0.1 */
+    int32_t engine;    /* DIMGPU_CG_ENGINE_*: how a solve runs when use_graph != 0 */
 } dimgpu_cg_params;
+
+#define DIMGPU_CG_ENGINE_AUTO 0  /* the library's choice: currently the graph (faster on every measured system) */
+#define DIMGPU_CG_ENGINE_GRAPH 1 /* one CUDA graph per solve: 3 kernels per iteration in a device-side loop */
+#define DIMGPU_CG_ENGINE_FUSED 2 /* one persistent cooperative kernel per solve, grid barriers between phases */
 
 typedef struct {
     int64_t iterations;      /* CG iterations (inner iterations for the mixed solver) */

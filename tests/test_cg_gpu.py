@@ -8,8 +8,9 @@ import oracle
 from diploma_research_gb300 import _native as N
 from diploma_research_gb300.cg import CGSolver, cg
 from diploma_research_gb300.csr5 import csr5
-from diploma_research_gb300.generators import laplacian_2d_5pt, rhs, stencil_3d_27pt
+from diploma_research_gb300.generators import laplacian_2d_5pt, power_law, rhs, stencil_3d_27pt
 from diploma_research_gb300.mat import csr, dimensions_t
+from helpers import random_csr
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 pytestmark = pytest.mark.gpu
@@ -34,13 +35,16 @@ def test_reference_fixture_cg(native):
     np.testing.assert_allclose(x, g["cg_x"], rtol=0, atol=1e-9)
 
 
-@pytest.mark.parametrize("use_graph", [True, False])
-def test_fp64_cg_vs_oracle(native, use_graph):
+ENGINES = [("graph", True), ("fused", True), ("graph", False)]  # (engine, use_graph): False = host loop
+
+
+@pytest.mark.parametrize("engine,use_graph", ENGINES)
+def test_fp64_cg_vs_oracle(native, engine, use_graph):
     m = laplacian_2d_5pt(64)
     xs, b = rhs(m, 0)
     xo, ito, relo = _oracle_cg(m, b, 1e-10)
     A = csr5.from_csr(m)
-    x, res = cg(A, b, tol=1e-10, use_graph=use_graph)
+    x, res = cg(A, b, tol=1e-10, use_graph=use_graph, engine=engine)
     assert res.converged and res.rel_residual <= 1.5e-10
     assert abs(res.iterations - ito) <= 2
     np.testing.assert_allclose(x, xo, rtol=0, atol=1e-8)
@@ -51,17 +55,66 @@ def test_graph_and_host_loop_agree_bitwise(native):
     m = laplacian_2d_5pt(48)
     _, b = rhs(m, 1)
     A = csr5.from_csr(m)
-    x1, r1 = cg(A, b, tol=1e-9, use_graph=True)
+    x1, r1 = cg(A, b, tol=1e-9, use_graph=True, engine="graph")
     x2, r2 = cg(A, b, tol=1e-9, use_graph=False)
     assert r1.iterations == r2.iterations
     assert np.array_equal(x1, x2)
 
 
-def test_device_buffers_and_nonzero_x0(native, torch_cuda):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_fused_is_reproducible_and_agrees_with_graph(native, precision):
+    m = laplacian_2d_5pt(80)
+    _, b = rhs(m, 5)
+    A = csr5.from_csr(m)
+    x1, r1 = cg(A, b, tol=1e-10, engine="fused", precision=precision)
+    x2, r2 = cg(A, b, tol=1e-10, engine="fused", precision=precision)
+    assert r1.iterations == r2.iterations and np.array_equal(x1, x2)  # fixed-order sums: bitwise repeatable
+    x3, r3 = cg(A, b, tol=1e-10, engine="graph", precision=precision)
+    assert r1.converged and r3.converged
+    assert abs(r1.iterations - r3.iterations) <= 2
+    assert np.linalg.norm(x1 - x3) / np.linalg.norm(x3) < 1e-8
+
+
+@pytest.mark.parametrize("n,density,long_rows,long_len,empty", [
+    (300, 3.0, 0, (64, 700), 0.0),          # tail only: no full tile
+    (700, 1.0, 0, (64, 700), 0.2),          # about one tile, empty rows
+    (20000, 6.0, 6, (600, 5000), 0.1),      # rows spanning many warps' runs, empty rows
+    (60000, 12.0, 20, (2000, 9000), 0.05),  # many long rows
+])
+def test_fused_spmv_phase(native, n, density, long_rows, long_len, empty):
+    """The persistent kernel's SpMV (look-back over warp runs, tail owner) on general matrices: with
+    max_it = 0 the solve stops after r0 = b - A x0, whose norm it reports."""
+    rng = np.random.default_rng(n)
+    m = random_csr(rng, n, n, density, empty_frac=empty, long_rows=long_rows, long_len=long_len)
+    A = csr5.from_csr(m)
+    x0 = rng.uniform(-1, 1, n)
+    b = rng.uniform(-1, 1, n)
+    for prec in ("fp64", "mixed"):
+        _, res = CGSolver(A, tol=0.0, max_it=0, engine="fused", precision=prec).solve(b, x0, raise_on_failure=False)
+        ref = np.linalg.norm(b - m.to_scipy() @ x0)
+        got = res.recurrence_rel_residual * np.linalg.norm(b)
+        assert abs(got - ref) <= 1e-12 * ref, (prec, got, ref)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_fused_power_law_cg(native, precision):
+    m = power_law(30000, 2.0, 3000, 7)
+    xs, b = rhs(m, 7)
+    A = csr5.from_csr(m)
+    x, res = cg(A, b, tol=1e-10, engine="fused", precision=precision)
+    assert res.converged and res.rel_residual <= 1e-10 * 1.01
+    xo, ito, _ = _oracle_cg(m, b, 1e-10)
+    if precision == "fp64":
+        assert abs(res.iterations - ito) <= 2
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-7
+
+
+@pytest.mark.parametrize("engine", ["graph", "fused"])
+def test_device_buffers_and_nonzero_x0(native, torch_cuda, engine):
     m = laplacian_2d_5pt(40)
     xs, b = rhs(m, 2)
     A = csr5.from_csr(m)
-    s = CGSolver(A, tol=1e-10)
+    s = CGSolver(A, tol=1e-10, engine=engine)
     bd = torch_cuda.tensor(b, device="cuda", dtype=torch_cuda.float64)
     xd = torch_cuda.tensor(xs + 0.01, device="cuda", dtype=torch_cuda.float64)
     s.solve(bd, xd)
@@ -72,11 +125,12 @@ def test_device_buffers_and_nonzero_x0(native, torch_cuda):
     assert res.iterations <= 1
 
 
-def test_mixed_precision_reaches_fp64_residual(native):
+@pytest.mark.parametrize("engine", ["graph", "fused"])
+def test_mixed_precision_reaches_fp64_residual(native, engine):
     m = laplacian_2d_5pt(96)
     xs, b = rhs(m, 3)
     A = csr5.from_csr(m)
-    x, res = cg(A, b, tol=1e-10, precision="mixed")
+    x, res = cg(A, b, tol=1e-10, precision="mixed", engine=engine)
     assert res.converged
     assert res.rel_residual <= 1e-10 * 1.01
     assert res.reliable_updates >= 1
@@ -86,34 +140,40 @@ def test_mixed_precision_reaches_fp64_residual(native):
     assert res.iterations <= 2 * ito
 
 
-def test_not_converged_and_breakdown(native):
+@pytest.mark.parametrize("engine", ["graph", "fused"])
+def test_not_converged_and_breakdown(native, engine):
     m = laplacian_2d_5pt(64)
     _, b = rhs(m, 4)
     A = csr5.from_csr(m)
-    x, res = CGSolver(A, tol=1e-14, max_it=5).solve(b, raise_on_failure=False)
+    x, res = CGSolver(A, tol=1e-14, max_it=5, engine=engine).solve(b, raise_on_failure=False)
     assert not res.converged and res.iterations == 5
     with pytest.raises(N.NotConvergedError):
-        CGSolver(A, tol=1e-14, max_it=5).solve(b)
+        CGSolver(A, tol=1e-14, max_it=5, engine=engine).solve(b)
     neg = csr(m.dimensions, -m.values, m.row_start_offsets, m.col_indices)  # negative definite
     An = csr5.from_csr(neg)
     with pytest.raises(N.BreakdownError):
-        cg(An, b, tol=1e-10)
+        cg(An, b, tol=1e-10, engine=engine)
+    # the solver stays usable after a breakdown
+    x, res = cg(A, b, tol=1e-10, engine=engine)
+    assert res.converged
 
 
-def test_zero_rhs(native):
+@pytest.mark.parametrize("engine", ["graph", "fused"])
+def test_zero_rhs(native, engine):
     m = laplacian_2d_5pt(16)
     A = csr5.from_csr(m)
-    x, res = cg(A, np.zeros(256), tol=1e-10)
+    x, res = cg(A, np.zeros(256), tol=1e-10, engine=engine)
     assert res.converged and res.iterations == 0 and np.all(x == 0)
 
 
 @pytest.mark.slow
+@pytest.mark.parametrize("engine", ["graph", "fused"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_stencil27_128_cg(native, precision):
+def test_stencil27_128_cg(native, precision, engine):
     m = stencil_3d_27pt(128)
     xs, b = rhs(m, 1)
     A = csr5.from_csr(m)
-    x, res = cg(A, b, tol=1e-10, precision=precision)
+    x, res = cg(A, b, tol=1e-10, precision=precision, engine=engine)
     assert res.converged and res.rel_residual <= 1e-10 * 1.01
     if precision == "fp64":
         xo, ito, _ = _oracle_cg(m, b, 1e-10)  # the reference's CG loop on the same system
