@@ -98,6 +98,41 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 }
 
 // ------------------------------------------------------------------------------------------------
+// Decoupled look-back between warp runs (spmv.cu, spmm.cu): each run release-stores a flag word
+// (launch epoch << 2 | fragment kind) after publishing the row fragment a later run needs.
+// ------------------------------------------------------------------------------------------------
+constexpr uint32_t kFragNone = 0, kFragCarry = 1, kFragThrough = 2;
+
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Bounded wait for run k's flag of this launch; returns its fragment kind, or kFragNone after recording
+// kStatusWaitTimeout.  Polls without acquire (no cache invalidation per poll), then one acquire.
+__device__ __forceinline__ uint32_t wait_run(const uint32_t* flag, uint32_t epoch, uint32_t* status) {
+    if ((ld_relaxed_u32(flag) >> 2) != epoch) {
+        const uint64_t t0 = global_ns();
+        while ((ld_relaxed_u32(flag) >> 2) != epoch) {
+            if (global_ns() - t0 > DIMGPU_WAIT_NS) {
+                record_status(status, kStatusWaitTimeout);
+                return kFragNone;
+            }
+        }
+    }
+    return ld_acquire_u32(flag) & 3u;
+}
+
+// ------------------------------------------------------------------------------------------------
 // L2 cache policies and the 1-D bulk copy global -> shared (TMA engine).
 // Addresses must be 16-byte aligned and the size a multiple of 16 bytes.
 // ------------------------------------------------------------------------------------------------

@@ -123,7 +123,7 @@ int launch_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calib
 int check_status(dimgpu_calibrator* cal, cudaStream_t stream);
 
 // spmm.cu: CSR5 SpMM (lanes = right-hand sides, one pass takes k <= 32 columns)
-constexpr int kSpmmShapes = 3;  // launch shapes the autotuner chooses from (warps per CTA x stages)
+constexpr int kSpmmShapes = 2;  // launch shapes the autotuner chooses from (warps per CTA x stages)
 struct spmm_args {
     const void* X = nullptr;
     void* Y = nullptr;
@@ -138,10 +138,11 @@ struct spmm_args {
 };
 struct spmm_scratch {
     uint32_t nslots = 0;
-    double* cal_val = nullptr;   // [nslots * 32]
-    uint32_t* cal_row = nullptr; // [nslots]
-    double* dot_part = nullptr;  // [nslots * 32]
-    uint32_t* counter = nullptr;
+    double* cal_val = nullptr;   // [nslots * 32] k-vector fragments of the warp runs
+    uint32_t* cal_row = nullptr; // [nslots] their rows
+    uint32_t* flag = nullptr;    // [nslots] (launch epoch << 2) | fragment kind
+    double* dot_part = nullptr;  // [nslots * 32] per-CTA partials of the per-column dots
+    uint32_t* counter = nullptr; // [4] ticket, -, run counter, launch epoch
     uint32_t* status = nullptr;
 };
 int prepare_spmm_kernels();

@@ -1,17 +1,23 @@
 // spmm.cu -- CSR5 SpMM on GB300: Y = A X for k right-hand sides (X, Y row-major, k <= 32 per pass).
 //
 // The matrix side is the SpMV's (spmv.cu): the same device layout, tiles streamed into shared memory
-// by cp.async.bulk on an mbarrier ring, each warp owning a contiguous run of tiles, a per-warp
-// calibrator slot for the row that began before the run, and the last CTA resolving the slots and
-// the CSR tail.  What changes is the role of the lanes: lane j is right-hand side j.  The warp walks
-// a tile's 512 elements in CSR order (tile column by tile column, csr5.h's element order before the
-// transpose); every element broadcasts its value and column index from shared memory and every lane
-// gathers X[col, j] -- one coalesced k-wide row per element -- and accumulates.  A set bit_flag bit
-// (uniform across the warp) closes the running row, written as one coalesced Y row.  Rows crossing
-// tiles go through the same in-order carry chain as the SpMV, with k-vectors.
+// by cp.async.bulk on an mbarrier ring, each warp owning a contiguous run of tiles, rows that cross runs
+// finished by a decoupled look-back, the CSR tail by the last CTA.
+//
+// Lanes.  A warp is split into G = 32 / KP lane groups (KP = k rounded up to 8, 16 or 32); lane j of
+// a group is right-hand side j.  Group g walks the tile elements of tile columns [g KP, (g+1) KP) --
+// 16 KP consecutive elements in CSR order -- one element per step: the element's value and column
+// index come from shared memory (16-byte loads of a whole tile column), every lane gathers X[col, j]
+// (one coalesced k-wide row per group) and accumulates.  So one warp step does G elements x KP
+// right-hand sides of useful work, and GB300's FP64 pipe (a warp-wide DFMA costs the same whatever
+// the number of active lanes) is kept full when k < 32.  A set bit_flag bit closes the group's
+// running row (written as one k-wide Y row); after the tile the groups' head and tail sums are joined
+// in group order with shuffles, which finishes the rows that span groups and yields the tile's head
+// and open segments for the in-order carry chain -- the same left-to-right sums as the SpMV.
 //
 // The optional epilogue of the block CG computes, per right-hand side, dot_j = sum_i X[i,j] Y[i,j]
-// and alpha_j = rr_j / dot_j (columns whose mask is clear are skipped).
+// (products and per-tile partial sums in the value type, accumulated in f64 across tiles and CTAs in
+// a fixed order) and alpha_j = rr_j / dot_j (columns whose mask is clear are skipped).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -43,10 +49,11 @@ struct spmm_params {
     uint32_t nwarps;
     const uint32_t* empty_rows;
     uint32_t n_empty;
-    double* cal_val;     // [nwarps * 32]
-    uint32_t* cal_row;   // [nwarps]
-    double* dot_part;    // [nwarps * 32]
-    uint32_t* counter;
+    double* frag_val;    // [nwarps * 32] the k-vector fragment a run publishes for a later run
+    uint32_t* frag_row;  // [nwarps]
+    uint32_t* flag;      // [nwarps] (epoch << 2) | fragment kind
+    double* cta_part;    // [grid * 32] per-CTA partials of the per-column dots
+    uint32_t* words;     // [0] completion ticket, [2] run counter, [3] launch epoch
     uint32_t* status;
     // block-CG epilogue (DOT): dot_out[j], alpha_out[j] = rr[j] / dot_out[j] where mask[j] != 0
     double* dot_out;
@@ -67,48 +74,90 @@ struct mm_geom {
     static constexpr uint32_t DBYTES = 32 * 4;
     static constexpr uint32_t STAGE = VBYTES + CBYTES + DBYTES;
     static constexpr desc_fields F = fields_for(kSigma, 32);
+    static constexpr uint32_t YMASK = (1u << F.yb) - 1u;
 };
 
-template <typename VT>
-__device__ __forceinline__ VT stage_val(const unsigned char* st, uint32_t c, uint32_t r) {
-    const VT* sv = reinterpret_cast<const VT*>(st);
-    return sizeof(VT) == 8 ? sv[pos_device_f64(c, r, 32)] : sv[pos_device_q32(c, r, 32)];
+// The 16 column indices of tile column c (device layout, layout.cuh) from the stage's index area.
+__device__ __forceinline__ void stage_cols(const unsigned char* cols, uint32_t c, uint32_t (&ci)[kSigma]) {
+    const uint4* sc = reinterpret_cast<const uint4*>(cols);
+#pragma unroll
+    for (int q = 0; q < kSigma / 4; ++q) {
+        const uint4 w = sc[q * 32 + c];
+        ci[4 * q + 0] = w.x;
+        ci[4 * q + 1] = w.y;
+        ci[4 * q + 2] = w.z;
+        ci[4 * q + 3] = w.w;
+    }
 }
 
-template <typename VT, int WPC, int STAGES, bool DOT>
-__global__ void __launch_bounds__(WPC * 32) k_spmm(const spmm_params<VT> p) {
+// The 16 values of tile column c from the stage's value area.
+template <typename VT>
+__device__ __forceinline__ void stage_vals(const unsigned char* st, uint32_t c, VT (&v)[kSigma]) {
+    if constexpr (sizeof(VT) == 8) {
+        const double2* sv = reinterpret_cast<const double2*>(st);
+#pragma unroll
+        for (int q = 0; q < kSigma / 2; ++q) {
+            const double2 d = sv[q * 32 + c];
+            v[2 * q + 0] = d.x;
+            v[2 * q + 1] = d.y;
+        }
+    } else {
+        const float4* sv = reinterpret_cast<const float4*>(st);
+#pragma unroll
+        for (int q = 0; q < kSigma / 4; ++q) {
+            const float4 d = sv[q * 32 + c];
+            v[4 * q + 0] = d.x;
+            v[4 * q + 1] = d.y;
+            v[4 * q + 2] = d.z;
+            v[4 * q + 3] = d.w;
+        }
+    }
+}
+
+template <typename VT, int KP, int WPC, int STAGES, bool DOT>
+__global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
     using G = mm_geom<VT>;
+    constexpr int NG = 32 / KP;  // lane groups per warp
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ uint32_t s_last;
+    __shared__ uint32_t s_last, s_cta, s_epoch;
     __shared__ double s_dot[WPC][32];
 
     if (p.halt && *reinterpret_cast<volatile const uint32_t*>(p.halt))
         return;
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const uint32_t gw = blockIdx.x * WPC + warp;
-    const bool active = lane < p.k;
+    const unsigned g = lane / KP, j = lane % KP;
+    const bool active = j < p.k;
+    if (threadIdx.x == 0) {
+        s_cta = atomicAdd(&p.words[2], 1u);
+        s_epoch = *reinterpret_cast<volatile const uint32_t*>(&p.words[3]) + 1u;
+    }
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem) + warp * STAGES;
     unsigned char* ring = smem + 128 * ((WPC * STAGES * 8 + 127) / 128) + (size_t)warp * STAGES * G::STAGE;
 
     // empty rows below the tail: zero rows of Y
     for (uint64_t i = blockIdx.x * (uint64_t)WPC + warp; i < p.n_empty; i += (uint64_t)gridDim.x * WPC)
-        if (active)
+        if (lane < p.k)
             p.Y[(uint64_t)p.empty_rows[i] * p.ldy + lane] = VT(0);
-
-    const uint64_t t_begin = min(p.T, (uint64_t)gw * p.tpw);
+    __syncthreads();
+    const uint32_t cta = s_cta;
+    const uint32_t epoch = (s_epoch & 0x3fffffffu) ? (s_epoch & 0x3fffffffu) : 1u;
+    const uint32_t run = cta * WPC + warp;
+    const uint64_t t_begin = min(p.T, (uint64_t)run * p.tpw);
     const uint64_t t_end = min(p.T, t_begin + p.tpw);
     const uint64_t pol_keep = policy_evict_last();
 
     double dot_acc = 0.0;
+    VT tdot = VT(0);  // this tile's share of the dot, folded into dot_acc once per tile
     bool open = false, cal_valid = false;
     VT carry = VT(0), cal = VT(0);
     uint32_t carry_row = 0, cal_row = 0;
 
-    auto write_row = [&](uint32_t row, VT val) {
-        if (active) {
-            st_keep(p.Y + (uint64_t)row * p.ldy + lane, val, pol_keep);
+    // k-wide row write by the lanes of one group (`mine`), with its share of the dot
+    auto put_row = [&](bool mine, uint32_t row, VT val) {
+        if (mine && active) {
+            st_keep(p.Y + (uint64_t)row * p.ldy + j, val, pol_keep);
             if constexpr (DOT)
-                dot_acc = fma((double)val, (double)ldg_x(p.X + (uint64_t)row * p.ldx + lane, pol_keep), dot_acc);
+                tdot = fma(val, ldg_x(p.X + (uint64_t)row * p.ldx + j, pol_keep), tdot);
         }
     };
 
@@ -147,7 +196,6 @@ __global__ void __launch_bounds__(WPC * 32) k_spmm(const spmm_params<VT> p) {
                 break;
             }
             const unsigned char* st = ring + (size_t)s * G::STAGE;
-            const uint32_t* sc = reinterpret_cast<const uint32_t*>(st + G::VBYTES);
             const uint32_t* sd = reinterpret_cast<const uint32_t*>(st + G::VBYTES + G::CBYTES);
             const bool dirty = (raw & kDirty) != 0;
             const uint32_t optr = dirty ? __ldg(&p.tdo_ptr[t]) : 0u;
@@ -156,50 +204,98 @@ __global__ void __launch_bounds__(WPC * 32) k_spmm(const spmm_params<VT> p) {
             };
             const bool capped = ((sd[0] >> (G::F.yb + G::F.sb)) & 1u) != 0;
 
+            // ---- this group's elements: tile columns [c0, c0 + KP) ----
+            const uint32_t c0 = g * KP;
+            // segments are numbered by the row starts after tile element 0 (y_offset counts element 0 once)
+            uint32_t seg = (c0 == 0) ? 0u : ((sd[c0] & G::YMASK) - 1u);
             VT acc = VT(0), head = VT(0);
-            uint32_t seg = 0;
-            // Column c's gathered X rows are fetched one column ahead (xa/xb), so the gathers of the next
-            // column are in flight while this one accumulates; values come from shared memory.
-            VT xa[kSigma], xb[kSigma];
-            auto fetch = [&](uint32_t c, VT (&x)[kSigma]) {
+            bool hs = false;
+            // gathers of tile column c into x (X[col, j] for its 16 elements)
+            auto gather = [&](uint32_t c, VT (&x)[kSigma]) {
+                uint32_t ci[kSigma];
+                stage_cols(st + G::VBYTES, c, ci);
 #pragma unroll
-                for (uint32_t r = 0; r < kSigma; ++r) {
-                    const uint32_t cc = sc[pos_device_q32(c, r, 32)];
-                    x[r] = active ? ldg_x(p.X + (uint64_t)cc * p.ldx + lane, pol_keep) : VT(0);
-                }
+                for (int r = 0; r < kSigma; ++r)
+                    x[r] = active ? ldg_x(p.X + (uint64_t)ci[r] * p.ldx + j, pol_keep) : VT(0);
             };
+            // the 16 elements of tile column c, in CSR order, with their gathered x
             auto walk = [&](uint32_t c, const VT (&x)[kSigma]) {
-                const uint32_t fl = (sd[c] >> (G::F.yb + G::F.sb)) & 0xFFFFu;
+                uint32_t fl = (sd[c] >> (G::F.yb + G::F.sb)) & 0xFFFFu;
+                if (c == 0)
+                    fl &= ~1u;  // element 0 opens segment 0 without closing anything
+                VT v[kSigma];
+                stage_vals<VT>(st, c, v);
 #pragma unroll
-                for (uint32_t r = 0; r < kSigma; ++r) {
-                    if (((fl >> r) & 1u) && (c | r)) {  // a row starts here: the running row closes
-                        if (seg == 0)
-                            head = acc;
+                for (int r = 0; r < kSigma; ++r) {
+                    if ((fl >> r) & 1u) {
+                        if (hs)
+                            put_row(true, row_of(seg), acc);  // a row that began in this group's range
                         else
-                            write_row(row_of(seg), acc);
+                            head = acc;
+                        hs = true;
                         ++seg;
                         acc = VT(0);
                     }
-                    acc = fma(stage_val<VT>(st, c, r), x[r], acc);
+                    acc = fma(v[r], x[r], acc);
                 }
             };
-            fetch(0, xa);
-            for (uint32_t c = 0; c < 32; c += 2) {
-                fetch(c + 1, xb);
-                walk(c, xa);
-                if (c + 2 < 32)
-                    fetch(c + 2, xa);
-                walk(c + 1, xb);
+            if constexpr (sizeof(VT) == 4) {
+                // f32: the next column's gathers are in flight while this one accumulates
+                VT xa[kSigma], xb[kSigma];
+                gather(c0, xa);
+#pragma unroll 1
+                for (uint32_t cc = 0; cc < (uint32_t)KP; cc += 2) {
+                    gather(c0 + cc + 1, xb);
+                    walk(c0 + cc, xa);
+                    if (cc + 2 < (uint32_t)KP)
+                        gather(c0 + cc + 2, xa);
+                    walk(c0 + cc + 1, xb);
+                }
+            } else {
+#pragma unroll 1
+                for (uint32_t cc = 0; cc < (uint32_t)KP; ++cc) {
+                    VT xv[kSigma];
+                    gather(c0 + cc, xv);
+                    walk(c0 + cc, xv);
+                }
             }
-            const uint32_t K = seg + 1;
-            const VT Lt = acc;
-            const VT H = (K == 1) ? Lt : head;
-            const uint32_t row_last = (K == 1) ? row_start : row_of(seg);
+            if (!hs)
+                head = acc;
 
+            // ---- join the groups in order: rows spanning groups, the tile's head and open segments ----
+            VT open_v = VT(0), H = VT(0);
+            uint32_t open_seg = 0;
+            bool closed0 = false;
+#pragma unroll
+            for (int gg = 0; gg < NG; ++gg) {
+                const int src = gg * KP + (int)j;
+                const uint32_t ghs = __shfl_sync(kFull, hs ? 1u : 0u, src);
+                const VT ghd = __shfl_sync(kFull, head, src);
+                const VT gtl = __shfl_sync(kFull, acc, src);
+                const uint32_t gseg = __shfl_sync(kFull, seg, src);
+                open_v += ghd;
+                if (ghs) {
+                    if (open_seg == 0) {
+                        H = open_v;
+                        closed0 = true;
+                    } else {
+                        put_row(g == (unsigned)gg, row_of(open_seg), open_v);
+                    }
+                    open_v = gtl;
+                    open_seg = gseg;
+                }
+            }
+            if (!closed0)
+                H = open_v;
+            const uint32_t K = open_seg + 1;
+            const VT Lt = open_v;
+            const uint32_t row_last = (K == 1) ? row_start : row_of(open_seg);
+
+            // ---- in-order carry chain over the warp's tiles (per right-hand side, same in every group) ----
             if (K == 1) {
                 if (capped) {
                     if (open)
-                        write_row(carry_row, carry);
+                        put_row(g == 0, carry_row, carry);
                     open = true;
                     carry = H;
                     carry_row = row_start;
@@ -213,10 +309,10 @@ __global__ void __launch_bounds__(WPC * 32) k_spmm(const spmm_params<VT> p) {
             } else {
                 if (capped) {
                     if (open)
-                        write_row(carry_row, carry);
-                    write_row(row_start, H);
+                        put_row(g == 0, carry_row, carry);
+                    put_row(g == 0, row_start, H);
                 } else if (open) {
-                    write_row(row_start, carry + H);
+                    put_row(g == 0, row_start, carry + H);
                 } else {
                     cal += H;
                     cal_row = row_start;
@@ -225,6 +321,10 @@ __global__ void __launch_bounds__(WPC * 32) k_spmm(const spmm_params<VT> p) {
                 open = true;
                 carry = Lt;
                 carry_row = row_last;
+            }
+            if constexpr (DOT) {
+                dot_acc += (double)tdot;
+                tdot = VT(0);
             }
             __syncwarp();
             if (lane == 0 && t + STAGES < t_end) {
@@ -237,90 +337,154 @@ __global__ void __launch_bounds__(WPC * 32) k_spmm(const spmm_params<VT> p) {
                 const uint64_t i2 = t2 - t_begin;
                 (void)mbar_wait_bounded(&bars[i2 % STAGES], (uint32_t)((i2 / STAGES) & 1), p.status);
             }
-        } else if (open) {
-            write_row(carry_row, carry);
+        }
+
+        // ---- rows that cross runs: publish this run's fragment, finish the rows that end here ----
+        bool cont_after;
+        if (t_end < p.T)
+            cont_after = ((__ldg(&p.desc[t_end * 32]) >> (G::F.yb + G::F.sb)) & 1u) == 0;
+        else
+            cont_after = p.tail_start < p.rows && (uint64_t)p.row_ptr[p.tail_start] != p.T * kTS;
+        const bool through = cal_valid && !open;
+        uint32_t kind = kFragNone;
+        if (open && cont_after)
+            kind = kFragCarry;
+        else if (through && cont_after)
+            kind = kFragThrough;
+        if (kind != kFragNone && g == 0) {
+            p.frag_val[(uint64_t)run * 32 + j] = (double)(kind == kFragCarry ? carry : cal);
+            if (j == 0)
+                p.frag_row[run] = kind == kFragCarry ? carry_row : cal_row;
+            __threadfence();
+        }
+        __syncwarp();
+        if (lane == 0)
+            st_release_u32(&p.flag[run], (epoch << 2) | kind);
+        if (open && !cont_after)
+            put_row(g == 0, carry_row, carry);
+        if (cal_valid && (!through || !cont_after)) {
+            // look back for the run where cal_row began, then add the fragments in run order
+            uint32_t first = run;
+            if (lane == 0) {
+                while (first > 0) {
+                    --first;
+                    const uint32_t kd = wait_run(&p.flag[first], epoch, p.status);
+                    if (__ldcg(&p.frag_row[first]) != cal_row || kd == kFragNone) {
+                        record_status(p.status, kStatusBadIndex);
+                        first = run;
+                        break;
+                    }
+                    if (kd == kFragCarry)
+                        break;
+                }
+            }
+            first = __shfl_sync(kFull, first, 0);
+            VT v = VT(0);
+            if (first < run) {
+                v = (VT)__ldcg(&p.frag_val[(uint64_t)first * 32 + j]);
+                for (uint32_t k2 = first + 1; k2 < run; ++k2)
+                    v += (VT)__ldcg(&p.frag_val[(uint64_t)k2 * 32 + j]);
+            }
+            put_row(g == 0, cal_row, v + cal);
         }
     }
-    p.cal_val[(uint64_t)gw * 32 + lane] = (double)cal;
-    if (lane == 0)
-        p.cal_row[gw] = cal_valid ? (cal_row | kDirty) : 0u;
-    if constexpr (DOT)
-        p.dot_part[(uint64_t)gw * 32 + lane] = dot_acc;
+    if constexpr (DOT) {
+        dot_acc += (double)tdot;
+        // sum over the groups (same right-hand side j), then per CTA in warp order
+#pragma unroll
+        for (int o = KP; o < 32; o <<= 1)
+            dot_acc += __shfl_xor_sync(kFull, dot_acc, o);
+        s_dot[warp][lane] = dot_acc;
+    }
 
-    // ---- last CTA: calibrator slots, CSR tail, per-column dots ----
-    __threadfence();
+    // ---- completion ticket; the last CTA computes the CSR tail and the per-column dots ----
     __syncthreads();
-    if (threadIdx.x == 0)
-        s_last = (atomicAdd(p.counter, 1u) == gridDim.x - 1) ? 1u : 0u;
+    if constexpr (DOT) {
+        if (threadIdx.x < 32) {
+            double d = 0.0;
+            for (int w = 0; w < WPC; ++w)
+                d += s_dot[w][threadIdx.x];
+            p.cta_part[(uint64_t)cta * 32 + threadIdx.x] = d;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = (atomicAdd(&p.words[0], 1u) == gridDim.x - 1) ? 1u : 0u;
+    }
     __syncthreads();
     if (!s_last)
         return;
     __threadfence();
 
     double fix_dot = 0.0;
-    for (uint32_t wi = warp; wi < p.nwarps; wi += WPC) {
-        const uint32_t cr = __ldcg(&p.cal_row[wi]);
-        if (!(cr & kDirty))
-            continue;
-        if (wi > 0 && __ldcg(&p.cal_row[wi - 1]) == cr)
-            continue;
-        const uint32_t R = cr & ~kDirty;
-        VT accr = active ? __ldcg(&p.Y[(uint64_t)R * p.ldy + lane]) : VT(0);
-        double added = 0.0;
-        for (uint32_t w2 = wi; w2 < p.nwarps; ++w2) {
-            if (__ldcg(&p.cal_row[w2]) != cr)
-                break;
-            const VT cv = (VT)__ldcg(&p.cal_val[(uint64_t)w2 * 32 + lane]);
-            accr += cv;
-            added += (double)cv;
-        }
-        if (active) {
-            p.Y[(uint64_t)R * p.ldy + lane] = accr;
-            if constexpr (DOT)
-                fix_dot += added * (double)p.X[(uint64_t)R * p.ldx + lane];
-        }
-    }
-    __syncthreads();
     const uint64_t first_tail = p.T * kTS;
+    const uint32_t nruns = p.T ? (uint32_t)((p.T + p.tpw - 1) / p.tpw) : 0u;
+    const bool lane_on = lane < p.k;
     for (uint64_t r = (uint64_t)p.tail_start + warp; r < p.rows; r += WPC) {
         const uint64_t s0 = (r == p.tail_start) ? first_tail : (uint64_t)p.row_ptr[r];
         const uint64_t e = p.row_ptr[r + 1];
         VT a = VT(0);
         for (uint64_t kk = s0; kk < e; ++kk)
-            if (active)
+            if (lane_on)
                 a = fma(p.vals[kk], p.X[(uint64_t)p.col[kk] * p.ldx + lane], a);
-        if (active) {
-            if (r == p.tail_start && (uint64_t)p.row_ptr[r] != first_tail)
-                p.Y[r * p.ldy + lane] = __ldcg(&p.Y[r * p.ldy + lane]) + a;
-            else
-                p.Y[r * p.ldy + lane] = a;
+        if (r == p.tail_start && (uint64_t)p.row_ptr[r] != first_tail && nruns > 0) {
+            uint32_t first = nruns;
+            if (lane == 0) {
+                while (first > 0) {
+                    --first;
+                    const uint32_t kd = wait_run(&p.flag[first], epoch, p.status);
+                    if (__ldcg(&p.frag_row[first]) != (uint32_t)r || kd == kFragNone) {
+                        record_status(p.status, kStatusBadIndex);
+                        first = nruns;
+                        break;
+                    }
+                    if (kd == kFragCarry)
+                        break;
+                }
+            }
+            first = __shfl_sync(kFull, first, 0);
+            if (first < nruns && lane_on) {
+                VT v = (VT)__ldcg(&p.frag_val[(uint64_t)first * 32 + lane]);
+                for (uint32_t k2 = first + 1; k2 < nruns; ++k2)
+                    v += (VT)__ldcg(&p.frag_val[(uint64_t)k2 * 32 + lane]);
+                a = v + a;
+            }
+        }
+        if (lane_on) {
+            p.Y[r * p.ldy + lane] = a;
             if constexpr (DOT)
                 fix_dot += (double)a * (double)p.X[r * p.ldx + lane];
         }
     }
     if constexpr (DOT) {
-        double part = fix_dot;
-        for (uint32_t wi = warp; wi < p.nwarps; wi += WPC)
-            part += __ldcg(&p.dot_part[(uint64_t)wi * 32 + lane]);
-        s_dot[warp][lane] = part;
         __syncthreads();
-        if (warp == 0 && active) {
+        s_dot[warp][lane] = fix_dot;
+        __syncthreads();
+        if (warp == 0) {
             double d = 0.0;
+            for (uint32_t c = 0; c < gridDim.x; ++c)
+                d += __ldcg(&p.cta_part[(uint64_t)c * 32 + lane]);
             for (int w = 0; w < WPC; ++w)
                 d += s_dot[w][lane];
-            if (p.dot_out)
-                p.dot_out[lane] = d;
-            if (p.alpha_out) {
-                const uint32_t* mk = p.mask ? p.mask + (p.mask_sel ? 32u * (*p.mask_sel) : 0u) : nullptr;
-                const bool on = !mk || mk[lane];
-                if (on && (!(d > 0.0) || !isfinite(d)))
-                    record_status(p.status, kStatusBreakdown);
-                p.alpha_out[lane] = (on && d > 0.0 && isfinite(d)) ? p.rr[lane] / d : 0.0;
+            if (lane_on) {
+                if (p.dot_out)
+                    p.dot_out[lane] = d;
+                if (p.alpha_out) {
+                    const uint32_t* mk = p.mask ? p.mask + (p.mask_sel ? 32u * (*p.mask_sel) : 0u) : nullptr;
+                    const bool on = !mk || mk[lane];
+                    if (on && (!(d > 0.0) || !isfinite(d)))
+                        record_status(p.status, kStatusBreakdown);
+                    p.alpha_out[lane] = (on && d > 0.0 && isfinite(d)) ? p.rr[lane] / d : 0.0;
+                }
             }
         }
     }
-    if (threadIdx.x == 0)
-        *p.counter = 0u;
+    if (threadIdx.x == 0) {
+        p.words[0] = 0u;
+        p.words[2] = 0u;
+        p.words[3] = epoch;
+    }
 }
 
 template <typename VT, int WPC, int STAGES>
@@ -328,13 +492,13 @@ constexpr size_t mm_smem() {
     return 128 * ((WPC * STAGES * 8 + 127) / 128) + (size_t)WPC * STAGES * mm_geom<VT>::STAGE;
 }
 
-template <typename VT, int WPC, int STAGES, bool DOT>
+template <typename VT, int KP, int WPC, int STAGES, bool DOT>
 cudaError_t mm_attr() {
-    return cudaFuncSetAttribute(k_spmm<VT, WPC, STAGES, DOT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(k_spmm<VT, KP, WPC, STAGES, DOT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)mm_smem<VT, WPC, STAGES>());
 }
 
-template <typename VT, int WPC, int STAGES, bool DOT>
+template <typename VT, int KP, int WPC, int STAGES, bool DOT>
 int mm_launch(const dimgpu_csr5* m, const VT* vals, const spmm_args& a, const spmm_scratch& sc, cudaStream_t st) {
     const spmv_plan pl = make_spmv_plan(m->tile_count, device_sm_count(m->device), WPC);
     if (pl.nwarps > sc.nslots)
@@ -360,10 +524,11 @@ int mm_launch(const dimgpu_csr5* m, const VT* vals, const spmm_args& a, const sp
     p.nwarps = pl.nwarps;
     p.empty_rows = m->empty_rows;
     p.n_empty = m->n_empty;
-    p.cal_val = sc.cal_val;
-    p.cal_row = sc.cal_row;
-    p.dot_part = sc.dot_part;
-    p.counter = sc.counter;
+    p.frag_val = sc.cal_val;
+    p.frag_row = sc.cal_row;
+    p.flag = sc.flag;
+    p.cta_part = sc.dot_part;
+    p.words = sc.counter;
     p.status = sc.status;
     p.dot_out = a.dot_out;
     p.rr = a.rr;
@@ -371,22 +536,47 @@ int mm_launch(const dimgpu_csr5* m, const VT* vals, const spmm_args& a, const sp
     p.mask = a.mask;
     p.mask_sel = a.mask_sel;
     p.halt = a.halt;
-    k_spmm<VT, WPC, STAGES, DOT><<<pl.grid, WPC * 32, mm_smem<VT, WPC, STAGES>(), st>>>(p);
+    k_spmm<VT, KP, WPC, STAGES, DOT><<<pl.grid, WPC * 32, mm_smem<VT, WPC, STAGES>(), st>>>(p);
     DG_CUDA(cudaGetLastError());
     return DIMGPU_OK;
 }
 
+template <typename VT, int KP, bool DOT>
+int mm_dispatch_kp(const dimgpu_csr5* m, const VT* vals, const spmm_args& a, const spmm_scratch& sc, int shape,
+                   cudaStream_t st) {
+    switch (shape) {
+    case 0:
+        return mm_launch<VT, KP, 8, 3, DOT>(m, vals, a, sc, st);
+    default:
+        return mm_launch<VT, KP, 16, 2, DOT>(m, vals, a, sc, st);
+    }
+}
+
+// Lane-group width for k right-hand sides.
+inline int kp_for(uint32_t k) { return k <= 8 ? 8 : (k <= 16 ? 16 : 32); }
+
 template <typename VT, bool DOT>
 int mm_dispatch(const dimgpu_csr5* m, const VT* vals, const spmm_args& a, const spmm_scratch& sc, int shape,
                 cudaStream_t st) {
-    switch (shape) {
-    case 0:
-        return mm_launch<VT, 8, 3, DOT>(m, vals, a, sc, st);
-    case 1:
-        return mm_launch<VT, 16, 2, DOT>(m, vals, a, sc, st);
+    switch (kp_for(a.k)) {
+    case 8:
+        return mm_dispatch_kp<VT, 8, DOT>(m, vals, a, sc, shape, st);
+    case 16:
+        return mm_dispatch_kp<VT, 16, DOT>(m, vals, a, sc, shape, st);
     default:
-        return mm_launch<VT, 12, 2, DOT>(m, vals, a, sc, st);
+        return mm_dispatch_kp<VT, 32, DOT>(m, vals, a, sc, shape, st);
     }
+}
+
+template <typename VT, bool DOT>
+cudaError_t mm_attrs() {
+    cudaError_t e;
+    if ((e = mm_attr<VT, 8, 8, 3, DOT>()) != cudaSuccess) return e;
+    if ((e = mm_attr<VT, 8, 16, 2, DOT>()) != cudaSuccess) return e;
+    if ((e = mm_attr<VT, 16, 8, 3, DOT>()) != cudaSuccess) return e;
+    if ((e = mm_attr<VT, 16, 16, 2, DOT>()) != cudaSuccess) return e;
+    if ((e = mm_attr<VT, 32, 8, 3, DOT>()) != cudaSuccess) return e;
+    return mm_attr<VT, 32, 16, 2, DOT>();
 }
 
 }  // namespace
@@ -395,18 +585,10 @@ int prepare_spmm_kernels() {
     static int done = 0;
     if (done)
         return DIMGPU_OK;
-    DG_CUDA((mm_attr<double, 8, 3, false>()));
-    DG_CUDA((mm_attr<double, 8, 3, true>()));
-    DG_CUDA((mm_attr<double, 16, 2, false>()));
-    DG_CUDA((mm_attr<double, 16, 2, true>()));
-    DG_CUDA((mm_attr<double, 12, 2, false>()));
-    DG_CUDA((mm_attr<double, 12, 2, true>()));
-    DG_CUDA((mm_attr<float, 8, 3, false>()));
-    DG_CUDA((mm_attr<float, 8, 3, true>()));
-    DG_CUDA((mm_attr<float, 16, 2, false>()));
-    DG_CUDA((mm_attr<float, 16, 2, true>()));
-    DG_CUDA((mm_attr<float, 12, 2, false>()));
-    DG_CUDA((mm_attr<float, 12, 2, true>()));
+    DG_CUDA((mm_attrs<double, false>()));
+    DG_CUDA((mm_attrs<double, true>()));
+    DG_CUDA((mm_attrs<float, false>()));
+    DG_CUDA((mm_attrs<float, true>()));
     done = 1;
     return DIMGPU_OK;
 }
@@ -414,7 +596,7 @@ int prepare_spmm_kernels() {
 uint32_t spmm_max_slots(const dimgpu_csr5* m) {
     const int sms = device_sm_count(m->device);
     uint32_t n = 1;
-    for (int wpc : {8, 12, 16})
+    for (int wpc : {8, 16})
         n = std::max<uint32_t>(n, make_spmv_plan(m->tile_count, sms, wpc).nwarps);
     return n;
 }
@@ -424,6 +606,8 @@ int spmm_scratch_init(spmm_scratch* s, const dimgpu_csr5* m) {
     DG_CHECK(dev_alloc_n(&s->cal_val, (uint64_t)s->nslots * 32));
     DG_CHECK(dev_alloc_n(&s->dot_part, (uint64_t)s->nslots * 32));
     DG_CHECK(dev_alloc_n(&s->cal_row, s->nslots));
+    DG_CHECK(dev_alloc_n(&s->flag, s->nslots));
+    DG_CUDA(cudaMemset(s->flag, 0, sizeof(uint32_t) * s->nslots));
     DG_CHECK(dev_alloc_n(&s->counter, 4));
     DG_CHECK(dev_alloc_n(&s->status, 4));
     DG_CUDA(cudaMemset(s->counter, 0, 16));
@@ -435,6 +619,7 @@ void spmm_scratch_release(spmm_scratch* s) {
     dev_free(s->cal_val);
     dev_free(s->dot_part);
     dev_free(s->cal_row);
+    dev_free(s->flag);
     dev_free(s->counter);
     dev_free(s->status);
     *s = spmm_scratch{};

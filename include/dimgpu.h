@@ -142,7 +142,7 @@ DIMGPU_API int dimgpu_csr5_spmm(const dimgpu_csr5* m, uint32_t k, const double* 
                                 uint64_t ldy, void* stream);
 DIMGPU_API int dimgpu_csr5_spmm_f32(const dimgpu_csr5* m, uint32_t k, const float* X, uint64_t ldx, float* Y,
                                     uint64_t ldy, void* stream);
-/* The launch shape the autotuner picked for (k, f32): 0..2, or -1 before the first call. */
+/* The launch shape the autotuner picked for (k, f32): 0 (8 warps x 3 stages) or 1 (16 x 2), -1 before the first call. */
 DIMGPU_API int dimgpu_csr5_spmm_shape(const dimgpu_csr5* m, uint32_t k, int f32, int* shape);
 
 /* ---- vectors (include/dim/vec.h:29-84), device memory ----------------------------------------- */

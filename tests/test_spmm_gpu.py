@@ -26,11 +26,11 @@ def _check(torch, m, k, seed=0, f32=False):
     tol = 1e-4 if f32 else 1e-12
     err = np.abs(Y - Y_ref)
     assert np.all(err <= tol * AX + 1e-300), float(np.max(err / (AX + 1e-300)))
-    assert spmm_shape(A, min(k, 32), f32) in (0, 1, 2)
+    assert spmm_shape(A, min(k, 32), f32) in (0, 1)
     return A
 
 
-@pytest.mark.parametrize("k", [1, 3, 8, 16, 32, 40])
+@pytest.mark.parametrize("k", [1, 3, 5, 8, 12, 16, 24, 32, 40])
 def test_spmm_random(native, torch_cuda, k):
     rng = np.random.default_rng(k)
     m = random_csr(rng, 5000, 4000, 12.0, empty_frac=0.1, long_rows=3, long_len=(700, 3000))
