@@ -112,19 +112,20 @@ __device__ __forceinline__ void set_ru(const vec_ctx& c, bool go) {
         cudaGraphSetConditional(c.ru, go ? 1u : 0u);
 }
 
-// Calls f(i) for every vector index i in [0, nv), kUnroll grid strides at a time so that each thread
-// keeps several independent 16-byte accesses in flight.
+// Calls f(i) for every vector index i in [0, nv): each thread takes kUnroll elements one grid stride
+// apart per round (guarded), so that their independent 16-byte loads are in flight together.  The grid
+// is sized (cg_vec_grid) so that most threads run a single round.
 template <typename F>
 __device__ __forceinline__ void vloop(uint64_t nv, F f) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    for (; i + (kUnroll - 1) * stride < nv; i += kUnroll * stride) {
+    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; base < nv; base += kUnroll * stride) {
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u)
-            f(i + u * stride);
+        for (int u = 0; u < kUnroll; ++u) {
+            const uint64_t i = base + u * stride;
+            if (i < nv)
+                f(i);
+        }
     }
-    for (; i < nv; i += stride)
-        f(i);
 }
 
 // The scalar elements past the last full vector, visited by the first threads of block 0.
@@ -147,8 +148,8 @@ __global__ void __launch_bounds__(kVecThreads) k_init64(const double* b, const d
     vloop(n / 2, [&](uint64_t i) {
         const double2 bi = ld2_keep(b + 2 * i, pol), ai = ld2_keep(Ax + 2 * i, pol);
         const double2 ri = make_double2(bi.x - ai.x, bi.y - ai.y);
-        st2_keep(r + 2 * i, ri, pol);
-        st2_keep(s + 2 * i, ri, pol);
+        st2_stream(r + 2 * i, ri, pol);
+        st2_stream(s + 2 * i, ri, pol);
         rr = fma(ri.x, ri.x, fma(ri.y, ri.y, rr));
         bb = fma(bi.x, bi.x, fma(bi.y, bi.y, bb));
     });
@@ -193,7 +194,7 @@ __global__ void __launch_bounds__(kVecThreads) k_update_r64(const double* As, do
         double2 q = ld2_keep(r + 2 * i, pol);
         q.x = fma(-alpha, a.x, q.x);
         q.y = fma(-alpha, a.y, q.y);
-        st2_keep(r + 2 * i, q, pol);
+        st2_stream(r + 2 * i, q, pol);
         rr = fma(q.x, q.x, fma(q.y, q.y, rr));
     });
     vtail(n, 2, [&](uint64_t i) {
@@ -231,8 +232,8 @@ __global__ void __launch_bounds__(kVecThreads) k_update_xs64(double* x, double* 
     if (more) {
         vloop(n / 2, [&](uint64_t i) {
             const double2 si = ld2_keep(s + 2 * i, pol), xi = ld2_keep(x + 2 * i, pol), ri = ld2_keep(r + 2 * i, pol);
-            st2_keep(x + 2 * i, make_double2(fma(alpha, si.x, xi.x), fma(alpha, si.y, xi.y)), pol);
-            st2_keep(s + 2 * i, make_double2(fma(beta, si.x, ri.x), fma(beta, si.y, ri.y)), pol);
+            st2_stream(x + 2 * i, make_double2(fma(alpha, si.x, xi.x), fma(alpha, si.y, xi.y)), pol);
+            st2_stream(s + 2 * i, make_double2(fma(beta, si.x, ri.x), fma(beta, si.y, ri.y)), pol);
         });
         vtail(n, 2, [&](uint64_t i) {
             const double si = s[i];
@@ -242,7 +243,7 @@ __global__ void __launch_bounds__(kVecThreads) k_update_xs64(double* x, double* 
     } else {
         vloop(n / 2, [&](uint64_t i) {
             const double2 si = ld2_keep(s + 2 * i, pol), xi = ld2_keep(x + 2 * i, pol);
-            st2_keep(x + 2 * i, make_double2(fma(alpha, si.x, xi.x), fma(alpha, si.y, xi.y)), pol);
+            st2_stream(x + 2 * i, make_double2(fma(alpha, si.x, xi.x), fma(alpha, si.y, xi.y)), pol);
         });
         vtail(n, 2, [&](uint64_t i) { x[i] = fma(alpha, s[i], x[i]); });
     }
@@ -264,9 +265,9 @@ __global__ void __launch_bounds__(kVecThreads) k_init_mixed(const double* b, con
         const double2 a0 = ld2_keep(Ax + 4 * i, pol), a1 = ld2_keep(Ax + 4 * i + 2, pol);
         const double r0 = b0.x - a0.x, r1 = b0.y - a0.y, r2 = b1.x - a1.x, r3 = b1.y - a1.y;
         const float4 rf = make_float4((float)r0, (float)r1, (float)r2, (float)r3);
-        st4_keep(r32 + 4 * i, rf, pol);
-        st4_keep(s32 + 4 * i, rf, pol);
-        st4_keep(y32 + 4 * i, make_float4(0.f, 0.f, 0.f, 0.f), pol);
+        st4_stream(r32 + 4 * i, rf, pol);
+        st4_stream(s32 + 4 * i, rf, pol);
+        st4_stream(y32 + 4 * i, make_float4(0.f, 0.f, 0.f, 0.f), pol);
         rr = fma(r0, r0, fma(r1, r1, fma(r2, r2, fma(r3, r3, rr))));
         bb = fma(b0.x, b0.x, fma(b0.y, b0.y, fma(b1.x, b1.x, fma(b1.y, b1.y, bb))));
     });
@@ -318,8 +319,8 @@ __global__ void __launch_bounds__(kVecThreads) k_update_r_mixed(const float* As,
         float4 q = ld4_keep(r + 4 * i, pol), yi = ld4_keep(y + 4 * i, pol);
         q = make_float4(fmaf(-af, a.x, q.x), fmaf(-af, a.y, q.y), fmaf(-af, a.z, q.z), fmaf(-af, a.w, q.w));
         yi = make_float4(fmaf(af, si.x, yi.x), fmaf(af, si.y, yi.y), fmaf(af, si.z, yi.z), fmaf(af, si.w, yi.w));
-        st4_keep(r + 4 * i, q, pol);
-        st4_keep(y + 4 * i, yi, pol);
+        st4_stream(r + 4 * i, q, pol);
+        st4_stream(y + 4 * i, yi, pol);
         rr += (double)sq4(q);
     });
     vtail(n, 4, [&](uint64_t i) {
@@ -353,9 +354,9 @@ __global__ void __launch_bounds__(kVecThreads) k_flush_mixed(double* x, float* y
     vloop(n / 4, [&](uint64_t i) {
         const float4 yi = ld4_keep(y + 4 * i, pol);
         const double2 x0 = ld2_keep(x + 4 * i, pol), x1 = ld2_keep(x + 4 * i + 2, pol);
-        st2_keep(x + 4 * i, make_double2(x0.x + (double)yi.x, x0.y + (double)yi.y), pol);
-        st2_keep(x + 4 * i + 2, make_double2(x1.x + (double)yi.z, x1.y + (double)yi.w), pol);
-        st4_keep(y + 4 * i, make_float4(0.f, 0.f, 0.f, 0.f), pol);
+        st2_stream(x + 4 * i, make_double2(x0.x + (double)yi.x, x0.y + (double)yi.y), pol);
+        st2_stream(x + 4 * i + 2, make_double2(x1.x + (double)yi.z, x1.y + (double)yi.w), pol);
+        st4_stream(y + 4 * i, make_float4(0.f, 0.f, 0.f, 0.f), pol);
     });
     vtail(n, 4, [&](uint64_t i) {
         x[i] += (double)y[i];
@@ -375,7 +376,7 @@ __global__ void __launch_bounds__(kVecThreads) k_ru_r_mixed(const double* b, con
         const double2 b0 = ld2_keep(b + 4 * i, pol), b1 = ld2_keep(b + 4 * i + 2, pol);
         const double2 a0 = ld2_keep(Ax + 4 * i, pol), a1 = ld2_keep(Ax + 4 * i + 2, pol);
         const double r0 = b0.x - a0.x, r1 = b0.y - a0.y, r2 = b1.x - a1.x, r3 = b1.y - a1.y;
-        st4_keep(r32 + 4 * i, make_float4((float)r0, (float)r1, (float)r2, (float)r3), pol);
+        st4_stream(r32 + 4 * i, make_float4((float)r0, (float)r1, (float)r2, (float)r3), pol);
         rr = fma(r0, r0, fma(r1, r1, fma(r2, r2, fma(r3, r3, rr))));
     });
     vtail(n, 4, [&](uint64_t i) {
@@ -411,7 +412,7 @@ __global__ void __launch_bounds__(kVecThreads) k_update_s_mixed(float* s, const 
     const uint64_t pol = policy_evict_last();
     vloop(n / 4, [&](uint64_t i) {
         const float4 si = ld4_keep(s + 4 * i, pol), ri = ld4_keep(r + 4 * i, pol);
-        st4_keep(s + 4 * i,
+        st4_stream(s + 4 * i,
                  make_float4(fmaf(beta, si.x, ri.x), fmaf(beta, si.y, ri.y), fmaf(beta, si.z, ri.z),
                              fmaf(beta, si.w, ri.w)),
                  pol);
@@ -724,7 +725,9 @@ int dimgpu_cg_create(const dimgpu_csr5* m, const dimgpu_cg_params* params, void*
         s->params.reliable_delta = 0.1;
     s->n = m->rows;
     const int sms = device_sm_count(m->device);
-    s->grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * 2, (s->n + kVecThreads - 1) / kVecThreads));
+    // enough blocks for one round of kUnroll f64 pairs per thread, at least one per SM
+    s->grid = (int)std::max<uint64_t>(
+        (uint64_t)sms, std::min<uint64_t>((uint64_t)sms * 8, (s->n / 2 + kUnroll * kVecThreads - 1) / (kUnroll * kVecThreads)));
     const uint64_t n = std::max<uint64_t>(4, s->n);
     int rc = DIMGPU_OK;
     do {

@@ -156,18 +156,19 @@ __device__ __forceinline__ float ldv(const float* p) {
     return v;
 }
 
-// f(i) for every vector index i < nv; kUnroll grid strides at a time.
+// f(i) for every vector index i < nv: kUnroll elements one grid stride apart per round (guarded), their
+// loads in flight together.
 template <typename F>
 __device__ __forceinline__ void vloop(uint64_t nv, F f) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    for (; i + (kUnroll - 1) * stride < nv; i += kUnroll * stride) {
+    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; base < nv; base += kUnroll * stride) {
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u)
-            f(i + u * stride);
+        for (int u = 0; u < kUnroll; ++u) {
+            const uint64_t i = base + u * stride;
+            if (i < nv)
+                f(i);
+        }
     }
-    for (; i < nv; i += stride)
-        f(i);
 }
 
 // The scalar elements past the last full vector, visited by the first threads of block 0.

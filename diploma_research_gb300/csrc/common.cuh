@@ -223,6 +223,15 @@ __device__ __forceinline__ void st2_keep(double* p, double2 v, uint64_t policy) 
     asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;" ::"l"(p), "d"(v.x), "d"(v.y), "l"(policy)
                  : "memory");
 }
+// Stores of streamed vector elements that order nothing else: volatile (never dropped) but without a
+// memory clobber, so the compiler may issue the next elements' loads ahead of them.
+__device__ __forceinline__ void st2_stream(double* p, double2 v, uint64_t policy) {
+    asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;" ::"l"(p), "d"(v.x), "d"(v.y), "l"(policy));
+}
+__device__ __forceinline__ void st4_stream(float* p, float4 v, uint64_t policy) {
+    asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "f"(v.x), "f"(v.y),
+                 "f"(v.z), "f"(v.w), "l"(policy));
+}
 __device__ __forceinline__ float4 ld4_keep(const float* p, uint64_t policy) {
     float4 v;
     asm("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
