@@ -247,6 +247,14 @@ int dimgpu_csr5_from_csr(uint32_t rows, uint32_t cols, uint64_t nnz, const uint3
         if ((rc = prepare_spmv_kernels()) != DIMGPU_OK) break;
         if ((rc = convert_csr5(m, d_rp, d_ci, d_v, s)) != DIMGPU_OK) break;
         m->plan = make_spmv_plan(m->tile_count, device_sm_count(m->device), 16);
+        {
+            // A matrix that fits in L2 together with the CG vectors (six f64 n-vectors) is better left
+            // there between products than streamed with an evict-first policy.
+            int l2 = 0;
+            cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, m->device);
+            const uint64_t matrix_bytes = m->nnz * 12 + (uint64_t)m->tile_count * 32 * 4;
+            m->keep_in_l2 = (l2 > 0 && matrix_bytes + 48ull * m->rows <= (uint64_t)l2) ? 1 : 0;
+        }
         m->plan32 = make_spmv_plan32(m->tile_count, device_sm_count(m->device));
         m->own_cal = new dimgpu_calibrator();
         if ((rc = calibrator_init(m->own_cal, m)) != DIMGPU_OK) break;

@@ -675,6 +675,7 @@ int launch_fused(dimgpu_cg_solver* s, cudaStream_t st) {
     a.nwarps = s->fwarps;
     a.tpw = a.T ? (a.T + a.nwarps - 1) / a.nwarps : 0;
     a.tail_warp = a.T ? (uint32_t)((a.T - 1) / a.tpw) : 0u;
+    a.keep_matrix = m->keep_in_l2;
     a.b = s->b;
     a.x = s->x;
     a.r = s->r;

@@ -46,6 +46,7 @@ struct cg_fused_args {
     uint64_t tpw;        // tiles per warp
     uint32_t nwarps;     // grid * warps per CTA
     uint32_t tail_warp;  // the warp that owns the last tile and computes the CSR tail
+    int keep_matrix;     // the matrix stays in L2 between products
     // vectors (n = rows)
     const double* b;
     double *x, *r, *s, *As, *Ax;

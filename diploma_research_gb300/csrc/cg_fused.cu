@@ -220,7 +220,7 @@ __device__ __noinline__ void spmv_phase(const cg_fused_args& p, const VT* vals, 
     const tile_io<VT> io{x, y, p.tdo_ptr, p.tdo, p.rows};
 
     if (t_begin < t_end) {
-        const uint64_t pol = policy_evict_first();
+        const uint64_t pol = p.keep_matrix ? policy_evict_normal() : policy_evict_first();
         auto stage_of = [&](uint64_t q) { return rs.ring + (size_t)(q % kFStages) * kStageStride; };
         auto issue = [&](uint64_t q, uint64_t t) {
             unsigned char* st = stage_of(q);

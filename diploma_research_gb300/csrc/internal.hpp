@@ -87,6 +87,7 @@ struct dimgpu_csr5 {
     int spmm_shape[2][33];       // autotuned SpMM launch shape per (f32?, k); -1 = not tuned yet
     void* spmm_sc = nullptr;     // the handle's own SpMM scratch (dimgpu::spmm_scratch), built on first use
     dimgpu_csr5* transposed = nullptr;  // A^T, built on first transpose use
+    int keep_in_l2 = 0;        // matrix + CG vectors fit in L2: stream the matrix without evict-first
     dimgpu::spmv_plan plan;    // f64 SpMV launch
     dimgpu::spmv_plan plan32;  // f32 SpMV launch (more warps per CTA)
     dimgpu_calibrator* own_cal = nullptr;

@@ -66,6 +66,7 @@ struct spmv_params {
     uint32_t nwarps;
     const uint32_t* empty_rows;
     uint32_t n_empty;
+    int keep_matrix;     // the matrix stays in L2 between products (no evict-first policy)
     double* frag_val;    // [nwarps] fragment a run publishes for a later run
     uint32_t* frag_row;  // [nwarps] its row
     uint32_t* flag;      // [nwarps] (epoch << 2) | fragment kind, release-stored after the fragment
@@ -140,7 +141,7 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
 
     if (t_begin < t_end) {
         const Word* gdesc = reinterpret_cast<const Word*>(p.desc);
-        const uint64_t pol = policy_evict_first();
+        const uint64_t pol = p.keep_matrix ? policy_evict_normal() : policy_evict_first();
         if (lane == 0) {
             for (int s = 0; s < STAGES; ++s)
                 mbar_init(&bars[s], 1);
@@ -331,6 +332,7 @@ int launch_cfg(const dimgpu_csr5* m, const VT* vals, const VT* x, VT* y, dimgpu_
     p.nwarps = pl.nwarps;
     p.empty_rows = m->empty_rows;
     p.n_empty = m->n_empty;
+    p.keep_matrix = m->keep_in_l2;
     p.frag_val = cal->cal_val;
     p.frag_row = cal->cal_row;
     p.flag = cal->flag;
