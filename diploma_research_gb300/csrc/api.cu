@@ -258,6 +258,7 @@ int dimgpu_csr5_from_csr(uint32_t rows, uint32_t cols, uint64_t nnz, const uint3
         m->plan32 = make_spmv_plan32(m->tile_count, device_sm_count(m->device));
         m->own_cal = new dimgpu_calibrator();
         if ((rc = calibrator_init(m->own_cal, m)) != DIMGPU_OK) break;
+        if (m->layout == kLayoutDevice && m->sigma == 16 && (rc = autotune_gathers(m, s)) != DIMGPU_OK) break;
     } while (false);
     if (mem == DIMGPU_MEM_HOST) {
         dev_free(d_ci);
@@ -436,3 +437,7 @@ int dimgpu_vec_dot(uint64_t n, const double* l, const double* r, double* out, vo
 }
 
 }  // extern "C"
+
+namespace dimgpu {
+int vec_fill(uint64_t n, double v, double* y, cudaStream_t stream) { return dimgpu_vec_set(n, v, y, stream); }
+}  // namespace dimgpu

@@ -245,7 +245,7 @@ __device__ __noinline__ void spmv_phase(const cg_fused_args& p, const VT* vals, 
             raw_next = (t + 2 <= p.T) ? __ldg(&p.tile_ptr[t + 2]) : 0u;
             if (!mbar_wait_bounded(&rs.bars[q % kFStages], (uint32_t)((q / kFStages) & 1), p.status))
                 break;
-            process_tile<VT, kSigma, DOT, true>(io, stage_of(q), lane, t, raw, raw_n, pol_keep, ch);
+            process_tile<VT, kSigma, DOT, kXCoherent>(io, stage_of(q), lane, t, raw, raw_n, pol_keep, ch);
             __syncwarp();
             if (lane == 0 && t + kFStages < t_end) {
                 fence_proxy_async_smem();
@@ -272,13 +272,13 @@ __device__ __noinline__ void spmv_phase(const cg_fused_args& p, const VT* vals, 
             const uint64_t e = p.row_ptr[r + 1];
             VT acc = VT(0);
             for (uint64_t k = s0; k < e; ++k)
-                acc = fma(vals[k], load_x<true>(x + p.col[k], pol_keep), acc);
+                acc = fma(vals[k], load_x<kXCoherent>(x + p.col[k], pol_keep), acc);
             if (r == p.tail_start && cont) {
                 tpart = acc;  // finishes the row the tiles left open
             } else {
                 y[r] = acc;
                 if constexpr (DOT)
-                    ch.dot_acc += (double)acc * (double)load_x<true>(x + r, pol_keep);
+                    ch.dot_acc += (double)acc * (double)load_x<kXCoherent>(x + r, pol_keep);
             }
         }
         tpart = __shfl_sync(kFull, tpart, 0);
@@ -312,7 +312,7 @@ __device__ __noinline__ void spmv_phase(const cg_fused_args& p, const VT* vals, 
             }
             y[ch.carry_row] = acc;
             if constexpr (DOT)
-                ch.dot_acc += (double)acc * (double)load_x<true>(x + ch.carry_row, pol_keep);
+                ch.dot_acc += (double)acc * (double)load_x<kXCoherent>(x + ch.carry_row, pol_keep);
         }
     }
     dot_lane += ch.dot_acc;

@@ -196,6 +196,19 @@ __device__ __forceinline__ float ldg_x(const float* p, uint64_t policy) {
     return v;
 }
 
+// Read-only gathers that skip L1 allocation: for matrices whose column indices have no locality (an
+// L1 line would be evicted before its next use), keeping L1 free for the stage traffic.
+__device__ __forceinline__ double ldg_x_stream(const double* p, uint64_t policy) {
+    double v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(policy));
+    return v;
+}
+__device__ __forceinline__ float ldg_x_stream(const float* p, uint64_t policy) {
+    float v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(policy));
+    return v;
+}
+
 // Coherent loads of data that the same (persistent) kernel wrote earlier, after a grid barrier: no
 // read-only path, and volatile so that the compiler never merges loads across loop iterations.
 __device__ __forceinline__ double ldc_x(const double* p, uint64_t policy) {

@@ -88,6 +88,7 @@ struct dimgpu_csr5 {
     void* spmm_sc = nullptr;     // the handle's own SpMM scratch (dimgpu::spmm_scratch), built on first use
     dimgpu_csr5* transposed = nullptr;  // A^T, built on first transpose use
     int keep_in_l2 = 0;        // matrix + CG vectors fit in L2: stream the matrix without evict-first
+    int x_mode = 0;            // how SpMV gathers x (spmv_tile.cuh: kXReadOnly or kXStream), autotuned
     dimgpu::spmv_plan plan;    // f64 SpMV launch
     dimgpu::spmv_plan plan32;  // f32 SpMV launch (more warps per CTA)
     dimgpu_calibrator* own_cal = nullptr;
@@ -122,6 +123,8 @@ int launch_spmv_f64(const dimgpu_csr5* m, const double* x, double* y, dimgpu_cal
 int launch_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calibrator* cal,
                     const spmv_epilogue& ep, cudaStream_t stream);
 int check_status(dimgpu_calibrator* cal, cudaStream_t stream);
+int autotune_gathers(dimgpu_csr5* m, cudaStream_t stream);
+int vec_fill(uint64_t n, double v, double* y, cudaStream_t stream);
 
 // spmm.cu: CSR5 SpMM (lanes = right-hand sides, one pass takes k <= 32 columns)
 constexpr int kSpmmShapes = 2;  // launch shapes the autotuner chooses from (warps per CTA x stages)

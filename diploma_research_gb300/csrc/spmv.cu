@@ -103,7 +103,7 @@ __device__ VT close_row(const spmv_params<VT>& p, uint32_t run, uint32_t R, VT o
     return acc + own;
 }
 
-template <typename VT, int SIGMA, int WPC, int STAGES, bool DOT>
+template <typename VT, int SIGMA, int WPC, int STAGES, bool DOT, int XM>
 __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
     using G = tile_geom<VT, SIGMA>;
     using Word = typename G::Word;
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
                 failed = true;
                 break;
             }
-            process_tile<VT, SIGMA, DOT>(io, ring + (size_t)s * G::STAGE, lane, t, raw, raw_n, pol_keep, ch);
+            process_tile<VT, SIGMA, DOT, XM>(io, ring + (size_t)s * G::STAGE, lane, t, raw, raw_n, pol_keep, ch);
 
             __syncwarp();
             if (lane == 0 && t + STAGES < t_end) {
@@ -343,7 +343,10 @@ int launch_cfg(const dimgpu_csr5* m, const VT* vals, const VT* x, VT* y, dimgpu_
     p.rr = ep.rr;
     p.alpha_out = ep.alpha_out;
     p.halt = ep.halt;
-    k_spmv<VT, SIGMA, WPC, STAGES, DOT><<<pl.grid, WPC * 32, smem, stream>>>(p);
+    if (m->x_mode == kXStream)
+        k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXStream><<<pl.grid, WPC * 32, smem, stream>>>(p);
+    else
+        k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXReadOnly><<<pl.grid, WPC * 32, smem, stream>>>(p);
     DG_CUDA(cudaGetLastError());
     return DIMGPU_OK;
 }
@@ -354,8 +357,13 @@ constexpr int kStages = 2;
 
 template <typename VT, int SIGMA, int WPC, int STAGES, bool DOT>
 cudaError_t set_smem_attr() {
-    return cudaFuncSetAttribute(k_spmv<VT, SIGMA, WPC, STAGES, DOT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem_bytes<VT, SIGMA, WPC, STAGES>());
+    const int bytes = (int)smem_bytes<VT, SIGMA, WPC, STAGES>();
+    cudaError_t e = cudaFuncSetAttribute(k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXReadOnly>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess)
+        return e;
+    return cudaFuncSetAttribute(k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXStream>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 }  // namespace
@@ -452,6 +460,46 @@ int launch_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calib
     default:
         return fail(DIMGPU_ERR_UNSUPPORTED, "sigma %u has no SpMV kernel", m->sigma);
     }
+}
+
+// Chooses how the x gathers load (kept in L1, or streamed past it) by timing both on this matrix: an
+// f64 SpMV of x = 1, the faster of two timed launches per mode.  Small matrices keep the default.
+int autotune_gathers(dimgpu_csr5* m, cudaStream_t stream) {
+    m->x_mode = kXReadOnly;
+    if (m->tile_count < 4096 || m->rows == 0 || m->cols == 0)
+        return DIMGPU_OK;
+    double *x = nullptr, *y = nullptr;
+    DG_CHECK(dev_alloc_n(&x, m->cols));
+    int rc = dev_alloc_n(&y, m->rows);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float best[2] = {1e30f, 1e30f};
+    if (rc == DIMGPU_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+        rc = cuda_fail(cudaGetLastError(), "cudaEventCreate");
+    if (rc == DIMGPU_OK)
+        rc = vec_fill(m->cols, 1.0, x, stream);
+    for (int mode = 0; mode < 2 && rc == DIMGPU_OK; ++mode) {
+        m->x_mode = mode == 0 ? kXReadOnly : kXStream;
+        for (int rep = 0; rep < 3 && rc == DIMGPU_OK; ++rep) {
+            cudaEventRecord(e0, stream);
+            rc = launch_spmv_f64(m, x, y, m->own_cal, spmv_epilogue{}, stream);
+            cudaEventRecord(e1, stream);
+            if (rc == DIMGPU_OK && cudaEventSynchronize(e1) == cudaSuccess && rep > 0) {
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                best[mode] = std::min(best[mode], ms);
+            }
+        }
+    }
+    if (rc == DIMGPU_OK)
+        rc = check_status(m->own_cal, stream);
+    m->x_mode = best[1] < 0.97f * best[0] ? kXStream : kXReadOnly;
+    if (e0)
+        cudaEventDestroy(e0);
+    if (e1)
+        cudaEventDestroy(e1);
+    dev_free(x);
+    dev_free(y);
+    return rc;
 }
 
 int check_status(dimgpu_calibrator* cal, cudaStream_t stream) {

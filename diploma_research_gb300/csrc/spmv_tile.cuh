@@ -92,24 +92,29 @@ struct tile_io {
     uint32_t rows;
 };
 
-// x loads: the read-only path for a kernel that never writes x (COH = false), coherent loads for the
-// persistent CG kernel, which rewrites x between its SpMV phases (COH = true).
-template <bool COH, typename VT>
+// How the x gathers load: the read-only path kept in L1 (matrices whose column indices have locality),
+// the read-only path without L1 allocation (no locality), or coherent loads for the persistent CG
+// kernel, which rewrites x between its SpMV phases.
+enum : int { kXReadOnly = 0, kXCoherent = 1, kXStream = 2 };
+
+template <int XM, typename VT>
 __device__ __forceinline__ VT load_x(const VT* p, uint64_t policy) {
-    if constexpr (COH)
+    if constexpr (XM == kXCoherent)
         return ldc_x(p, policy);
+    else if constexpr (XM == kXStream)
+        return ldg_x_stream(p, policy);
     else
         return ldg_x(p, policy);
 }
 
 // Writes a row the chain closed (lane 0) and accumulates its share of x.y.
-template <typename VT, bool DOT, bool COH = false>
+template <typename VT, bool DOT, int XM = kXReadOnly>
 __device__ __forceinline__ void chain_write_row(const tile_io<VT>& io, warp_chain<VT>& ch, unsigned lane,
                                                 uint32_t row, VT val) {
     if (lane == 0) {
         io.y[row] = val;
         if constexpr (DOT) {
-            if constexpr (COH)
+            if constexpr (XM == kXCoherent)
                 ch.dot_acc += (double)val * (double)ldc_x(io.x + row, policy_evict_last());
             else
                 ch.dot_acc += (double)val * (double)ldg_keep(io.x + row);
@@ -120,7 +125,7 @@ __device__ __forceinline__ void chain_write_row(const tile_io<VT>& io, warp_chai
 // Processes tile t staged at `st` (its values, column indices and descriptor words).  raw / raw_next are
 // tile_ptr[t] and tile_ptr[t + 1] with their dirty bits.  The stage's value area is reused as the
 // staging buffer of the tile's closed rows; the caller must __syncwarp() before refilling the stage.
-template <typename VT, int SIGMA, bool DOT, bool COH = false>
+template <typename VT, int SIGMA, bool DOT, int XM = kXReadOnly>
 __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned char* st, unsigned lane, uint64_t t,
                                              uint32_t raw, uint32_t raw_next, uint64_t pol_keep, warp_chain<VT>& ch) {
     using G = tile_geom<VT, SIGMA>;
@@ -136,12 +141,12 @@ __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned cha
     VT xv[SIGMA];
 #pragma unroll
     for (int r = 0; r < SIGMA; ++r)
-        xv[r] = load_x<COH>(io.x + ci[r], pol_keep);
+        xv[r] = load_x<XM>(io.x + ci[r], pol_keep);
     // the fused dot needs x at this tile's rows: fetch them now, off the write-out's path
     VT xrow = VT(0);
     if constexpr (DOT) {
         if (row_start + lane < io.rows)
-            xrow = load_x<COH>(io.x + row_start + lane, pol_keep);
+            xrow = load_x<XM == kXCoherent ? kXCoherent : kXReadOnly>(io.x + row_start + lane, pol_keep);
     }
     const uint32_t flag = (uint32_t)((uint64_t(w) >> (G::F.yb + G::F.sb)) & G::FMASK);
     const bool capped = (__shfl_sync(kFull, flag, 0) & 1u) != 0;
@@ -224,7 +229,7 @@ __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned cha
     if (K == 1) {
         if (capped) {
             if (ch.open)
-                chain_write_row<VT, DOT, COH>(io, ch, lane, ch.carry_row, ch.carry);
+                chain_write_row<VT, DOT, XM>(io, ch, lane, ch.carry_row, ch.carry);
             ch.open = true;
             ch.carry = H;
             ch.carry_row = row_start;
@@ -238,7 +243,7 @@ __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned cha
     } else {
         if (capped || ch.open) {
             if (capped && ch.open)
-                chain_write_row<VT, DOT, COH>(io, ch, lane, ch.carry_row, ch.carry);
+                chain_write_row<VT, DOT, XM>(io, ch, lane, ch.carry_row, ch.carry);
             if (!capped && lane == 0)
                 ystage[0] = ch.carry + H;  // the row that began before this tile closes here
             head_staged = true;
@@ -264,7 +269,7 @@ __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned cha
             st_keep(io.y + row, val, pol_keep);
             if constexpr (DOT) {
                 const bool have = !dirty && j == lo + lane && lane + lo < 32;
-                const VT xr = have ? xfirst : load_x<COH>(io.x + row, pol_keep);
+                const VT xr = have ? xfirst : load_x<XM == kXCoherent ? kXCoherent : kXReadOnly>(io.x + row, pol_keep);
                 ch.dot_acc = fma((double)val, (double)xr, ch.dot_acc);
             }
         }
