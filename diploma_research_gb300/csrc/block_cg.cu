@@ -138,7 +138,7 @@ __device__ __forceinline__ void batched_loop(uint64_t total, L load, O op) {
 
 // ---- FP64 ---------------------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(kThreads) k_bcg_init64(const double* B, const double* AX, double* R, double* S,
+__global__ void __launch_bounds__(kThreads, 2) k_bcg_init64(const double* B, const double* AX, double* R, double* S,
                                                          uint64_t total, bctx c) {
     const uint32_t kp = c.st->kp, k = c.st->k;
     const uint32_t j = threadIdx.x % kp;
@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(kThreads) k_bcg_init64(const double* B, const 
     (void)j;
 }
 
-__global__ void __launch_bounds__(kThreads) k_bcg_update_r64(const double* AS, double* R, uint64_t total, bctx c) {
+__global__ void __launch_bounds__(kThreads, 2) k_bcg_update_r64(const double* AS, double* R, uint64_t total, bctx c) {
     const uint32_t kp = c.st->kp, k = c.st->k, ph = c.st->phase;
     const uint32_t j = threadIdx.x % kp;
     const bool act = c.cols->masks[ph][j] != 0;
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(kThreads) k_bcg_update_r64(const double* AS, d
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_bcg_update_xs64(double* X, double* S, const double* R, uint64_t total,
+__global__ void __launch_bounds__(kThreads, 2) k_bcg_update_xs64(double* X, double* S, const double* R, uint64_t total,
                                                               const bcg_state* st, const bcg_cols* cols) {
     const uint32_t kp = st->kp, q = st->phase;
     const uint32_t j = threadIdx.x % kp;
@@ -234,8 +234,8 @@ __global__ void __launch_bounds__(kThreads) k_bcg_update_xs64(double* X, double*
     const double alpha = cols->alpha[j], beta = cols->beta[j];
     if (!was)
         return;
-    double sv[8], xv[8], rv[8];
-    batched_loop<8>(
+    double sv[4], xv[4], rv[4];
+    batched_loop<4>(
         total,
         [&](uint64_t f, int u) {
             sv[u] = S[f];
@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(kThreads) k_bcg_update_xs64(double* X, double*
 
 // ---- mixed --------------------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(kThreads) k_bcg_init_mixed(const double* B, const double* AX, float* R, float* S,
+__global__ void __launch_bounds__(kThreads, 2) k_bcg_init_mixed(const double* B, const double* AX, float* R, float* S,
                                                              float* Y, uint64_t total, bctx c) {
     const uint32_t kp = c.st->kp, k = c.st->k;
     double rr = 0, bb = 0;
@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(kThreads) k_bcg_init_mixed(const double* B, co
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_bcg_update_r_mixed(const float* AS, float* R, const float* S, float* Y,
+__global__ void __launch_bounds__(kThreads, 2) k_bcg_update_r_mixed(const float* AS, float* R, const float* S, float* Y,
                                                                  uint64_t total, bctx c) {
     const uint32_t kp = c.st->kp, k = c.st->k, ph = c.st->phase;
     const uint32_t j = threadIdx.x % kp;
@@ -300,8 +300,8 @@ __global__ void __launch_bounds__(kThreads) k_bcg_update_r_mixed(const float* AS
     const float af = (float)c.cols->alpha[j];
     double rr = 0;
     if (act) {
-        float a[16], q[16], sv[16], yv[16];
-        batched_loop<16>(
+        float a[4], q[4], sv[4], yv[4];
+        batched_loop<4>(
             total,
             [&](uint64_t f, int u) {
                 a[u] = AS[f];
@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(kThreads) k_bcg_update_r_mixed(const float* AS
 }
 
 // X += Y; Y = 0 (guarded: only during a reliable update)
-__global__ void __launch_bounds__(kThreads) k_bcg_flush(double* X, float* Y, uint64_t total, const bcg_state* st,
+__global__ void __launch_bounds__(kThreads, 2) k_bcg_flush(double* X, float* Y, uint64_t total, const bcg_state* st,
                                                         int guarded) {
     if (guarded && st->no_ru)
         return;
@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(kThreads) k_bcg_flush(double* X, float* Y, uin
 }
 
 // reliable update: R = B - AX for the active columns, true residuals, convergence per column
-__global__ void __launch_bounds__(kThreads) k_bcg_ru(const double* B, const double* AX, float* R, uint64_t total,
+__global__ void __launch_bounds__(kThreads, 2) k_bcg_ru(const double* B, const double* AX, float* R, uint64_t total,
                                                      bctx c) {
     if (c.st->no_ru)
         return;
@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(kThreads) k_bcg_ru(const double* B, const doub
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_bcg_update_s_mixed(float* S, const float* R, uint64_t total,
+__global__ void __launch_bounds__(kThreads, 2) k_bcg_update_s_mixed(float* S, const float* R, uint64_t total,
                                                                  const bcg_state* st, const bcg_cols* cols) {
     const uint32_t kp = st->kp, q = st->phase;
     const uint32_t j = threadIdx.x % kp;
@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(kThreads) k_bcg_update_s_mixed(float* S, const
 }
 
 // per-column ||B - AX||^2 and ||B||^2 (diagnostics, fixed order through grid_reduce_cols)
-__global__ void __launch_bounds__(kThreads) k_bcg_norms(const double* B, const double* AX, uint64_t total, bctx c,
+__global__ void __launch_bounds__(kThreads, 2) k_bcg_norms(const double* B, const double* AX, uint64_t total, bctx c,
                                                         double* out /* [2][32] */) {
     const uint32_t kp = c.st->kp;
     double rr = 0, bb = 0;

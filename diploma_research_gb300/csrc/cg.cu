@@ -112,15 +112,15 @@ __device__ __forceinline__ void set_ru(const vec_ctx& c, bool go) {
         cudaGraphSetConditional(c.ru, go ? 1u : 0u);
 }
 
-// Calls f(i) for every vector index i in [0, nv): each thread takes kUnroll elements one grid stride
-// apart per round (guarded), so that their independent 16-byte loads are in flight together.  The grid
-// is sized (cg_vec_grid) so that most threads run a single round.
-template <typename F>
+// Calls f(i) for every vector index i in [0, nv): each thread takes U elements one grid stride apart
+// per round (guarded), so that their independent 16-byte loads are in flight together.  The grid is two
+// resident blocks per SM (every kernel here is register-bounded to allow that), so one wave covers it.
+template <int U = kUnroll, typename F>
 __device__ __forceinline__ void vloop(uint64_t nv, F f) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; base < nv; base += kUnroll * stride) {
+    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; base < nv; base += U * stride) {
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u) {
+        for (int u = 0; u < U; ++u) {
             const uint64_t i = base + u * stride;
             if (i < nv)
                 f(i);
@@ -141,7 +141,7 @@ __device__ __forceinline__ void vtail(uint64_t n, uint64_t width, F f) {
 // ---------------------------------------------------------------------------------------------
 
 // r = b - Ax; s = r; rr = r.r; bb = b.b
-__global__ void __launch_bounds__(kVecThreads) k_init64(const double* b, const double* Ax, double* r, double* s,
+__global__ void __launch_bounds__(kVecThreads, 2) k_init64(const double* b, const double* Ax, double* r, double* s,
                                                         uint64_t n, vec_ctx c) {
     const uint64_t pol = policy_evict_last();
     double rr = 0, bb = 0;
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(kVecThreads) k_init64(const double* b, const d
 }
 
 // r -= alpha As; rr' = r.r; decide
-__global__ void __launch_bounds__(kVecThreads) k_update_r64(const double* As, double* r, uint64_t n, vec_ctx c) {
+__global__ void __launch_bounds__(kVecThreads, 2) k_update_r64(const double* As, double* r, uint64_t n, vec_ctx c) {
     cg_state* st = c.st;
     // the state was written by earlier kernels: read it once, both words in flight together
     const uint32_t stop = st->stop;
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(kVecThreads) k_update_r64(const double* As, do
 }
 
 // x += alpha s; s = r + beta s (the latter only while the solve continues)
-__global__ void __launch_bounds__(kVecThreads) k_update_xs64(double* x, double* s, const double* r, uint64_t n,
+__global__ void __launch_bounds__(kVecThreads, 2) k_update_xs64(double* x, double* s, const double* r, uint64_t n,
                                                              const cg_state* st) {
     const uint32_t pending = st->x_pending, stop = st->stop;
     const double alpha = st->alpha, beta = st->beta;
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(kVecThreads) k_update_xs64(double* x, double* 
     const uint64_t pol = policy_evict_last();
     const bool more = !stop;
     if (more) {
-        vloop(n / 2, [&](uint64_t i) {
+        vloop<2>(n / 2, [&](uint64_t i) {
             const double2 si = ld2_keep(s + 2 * i, pol), xi = ld2_keep(x + 2 * i, pol), ri = ld2_keep(r + 2 * i, pol);
             st2_stream(x + 2 * i, make_double2(fma(alpha, si.x, xi.x), fma(alpha, si.y, xi.y)), pol);
             st2_stream(s + 2 * i, make_double2(fma(beta, si.x, ri.x), fma(beta, si.y, ri.y)), pol);
@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(kVecThreads) k_update_xs64(double* x, double* 
             s[i] = fma(beta, si, r[i]);
         });
     } else {
-        vloop(n / 2, [&](uint64_t i) {
+        vloop<2>(n / 2, [&](uint64_t i) {
             const double2 si = ld2_keep(s + 2 * i, pol), xi = ld2_keep(x + 2 * i, pol);
             st2_stream(x + 2 * i, make_double2(fma(alpha, si.x, xi.x), fma(alpha, si.y, xi.y)), pol);
         });
@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(kVecThreads) k_update_xs64(double* x, double* 
 __device__ __forceinline__ float sq4(float4 v) { return fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, v.w * v.w))); }
 
 // r64 = b - Ax; r32 = s32 = r64; y32 = 0; rr = r64.r64; bb = b.b
-__global__ void __launch_bounds__(kVecThreads) k_init_mixed(const double* b, const double* Ax, float* r32, float* s32,
+__global__ void __launch_bounds__(kVecThreads, 2) k_init_mixed(const double* b, const double* Ax, float* r32, float* s32,
                                                             float* y32, uint64_t n, vec_ctx c) {
     const uint64_t pol = policy_evict_last();
     double rr = 0, bb = 0;
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(kVecThreads) k_init_mixed(const double* b, con
 
 // r32 -= alpha As32; y32 += alpha s32; rr' = r32.r32 (f32 partials of 4, summed in f64); decide whether a
 // reliable update is due
-__global__ void __launch_bounds__(kVecThreads) k_update_r_mixed(const float* As, float* r, const float* s, float* y,
+__global__ void __launch_bounds__(kVecThreads, 2) k_update_r_mixed(const float* As, float* r, const float* s, float* y,
                                                                 uint64_t n, vec_ctx c) {
     cg_state* st = c.st;
     const uint32_t stop = st->stop;
@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(kVecThreads) k_update_r_mixed(const float* As,
 }
 
 // x += y; y = 0 (at reliable updates and at the end of the solve)
-__global__ void __launch_bounds__(kVecThreads) k_flush_mixed(double* x, float* y, uint64_t n, const cg_state* st,
+__global__ void __launch_bounds__(kVecThreads, 2) k_flush_mixed(double* x, float* y, uint64_t n, const cg_state* st,
                                                              int guarded) {
     if (guarded && *reinterpret_cast<const volatile uint32_t*>(&st->no_ru))
         return;
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(kVecThreads) k_flush_mixed(double* x, float* y
 }
 
 // reliable update, after Ax = A x in f64: r32 = b - Ax; decide convergence on the true residual
-__global__ void __launch_bounds__(kVecThreads) k_ru_r_mixed(const double* b, const double* Ax, float* r32, uint64_t n,
+__global__ void __launch_bounds__(kVecThreads, 2) k_ru_r_mixed(const double* b, const double* Ax, float* r32, uint64_t n,
                                                             vec_ctx c) {
     cg_state* st = c.st;
     if (*reinterpret_cast<volatile uint32_t*>(&st->no_ru))
@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(kVecThreads) k_ru_r_mixed(const double* b, con
 }
 
 // s32 = r32 + beta s32 while the solve continues
-__global__ void __launch_bounds__(kVecThreads) k_update_s_mixed(float* s, const float* r, uint64_t n,
+__global__ void __launch_bounds__(kVecThreads, 2) k_update_s_mixed(float* s, const float* r, uint64_t n,
                                                                 const cg_state* st) {
     const uint32_t stop = st->stop;
     const float beta = (float)st->beta;
@@ -726,9 +726,9 @@ int dimgpu_cg_create(const dimgpu_csr5* m, const dimgpu_cg_params* params, void*
         s->params.reliable_delta = 0.1;
     s->n = m->rows;
     const int sms = device_sm_count(m->device);
-    // enough blocks for one round of kUnroll f64 pairs per thread, at least one per SM
+    // two resident blocks per SM (fewer for short vectors)
     s->grid = (int)std::max<uint64_t>(
-        (uint64_t)sms, std::min<uint64_t>((uint64_t)sms * 8, (s->n / 2 + kUnroll * kVecThreads - 1) / (kUnroll * kVecThreads)));
+        1, std::min<uint64_t>((uint64_t)sms * 2, (s->n / 2 + kVecThreads - 1) / kVecThreads));
     const uint64_t n = std::max<uint64_t>(4, s->n);
     int rc = DIMGPU_OK;
     do {
