@@ -4,16 +4,19 @@
 // by cp.async.bulk on an mbarrier ring, each warp owning a contiguous run of tiles, rows that cross runs
 // finished by a decoupled look-back, the CSR tail by the last CTA.
 //
-// Lanes.  A warp is split into G = 32 / KP lane groups (KP = k rounded up to 8, 16 or 32); lane j of
-// a group is right-hand side j.  Group g walks the tile elements of tile columns [g KP, (g+1) KP) --
-// 16 KP consecutive elements in CSR order -- one element per step: the element's value and column
-// index come from shared memory (16-byte loads of a whole tile column), every lane gathers X[col, j]
-// (one coalesced k-wide row per group) and accumulates.  So one warp step does G elements x KP
-// right-hand sides of useful work, and GB300's FP64 pipe (a warp-wide DFMA costs the same whatever
-// the number of active lanes) is kept full when k < 32.  A set bit_flag bit closes the group's
-// running row (written as one k-wide Y row); after the tile the groups' head and tail sums are joined
-// in group order with shuffles, which finishes the rows that span groups and yields the tile's head
-// and open segments for the in-order carry chain -- the same left-to-right sums as the SpMV.
+// Lanes.  KP = k rounded up to 8, 16 or 32.  Each lane holds V consecutive right-hand sides (f32: V = KP / 8
+// when k and the leading dimensions allow 8- or 16-byte vector accesses; else, and for FP64, V = 1), so a
+// lane group has LG = KP / V lanes and a warp G = 32 / LG groups; lane j of a group holds right-hand
+// sides [j V, (j+1) V).  Group g walks the tile elements of tile columns [g LG, (g+1) LG) -- 16 LG consecutive
+// elements in CSR order -- one element per step: the element's value and column index come from shared
+// memory (16-byte loads of a whole tile column), every lane gathers X[col, jV .. jV+V) (one coalesced
+// k-wide row per group) and accumulates.  So one warp step does G elements x KP right-hand sides of
+// useful work: GB300's FP64 pipe (a warp-wide DFMA costs the same whatever the number of active lanes)
+// is kept full when k < 32, and with V > 1 the per-element overhead (flags, shared loads, shuffles) is
+// shared by four elements also at k = 16 and 32.  A set bit_flag bit closes the group's running row
+// (written as one k-wide Y row); after the tile the groups' head and tail sums are joined in group order
+// with shuffles, which finishes the rows that span groups and yields the tile's head and open segments
+// for the in-order carry chain -- the same left-to-right sums as the SpMV.
 //
 // The optional epilogue of the block CG computes, per right-hand side, dot_j = sum_i X[i,j] Y[i,j]
 // (products and per-tile partial sums in the value type, accumulated in f64 across tiles and CTAs in
@@ -114,10 +117,93 @@ __device__ __forceinline__ void stage_vals(const unsigned char* st, uint32_t c, 
     }
 }
 
-template <typename VT, int KP, int WPC, int STAGES, bool DOT>
+// V consecutive right-hand sides of one lane.
+template <typename VT, int V>
+struct vv {
+    VT a[V];
+};
+
+template <typename VT, int V>
+__device__ __forceinline__ vv<VT, V> vv_zero() {
+    vv<VT, V> r;
+#pragma unroll
+    for (int i = 0; i < V; ++i)
+        r.a[i] = VT(0);
+    return r;
+}
+template <typename VT, int V>
+__device__ __forceinline__ void vv_add(vv<VT, V>& d, const vv<VT, V>& b) {
+#pragma unroll
+    for (int i = 0; i < V; ++i)
+        d.a[i] += b.a[i];
+}
+template <typename VT, int V>
+__device__ __forceinline__ vv<VT, V> vv_sum(const vv<VT, V>& x, const vv<VT, V>& y) {
+    vv<VT, V> r;
+#pragma unroll
+    for (int i = 0; i < V; ++i)
+        r.a[i] = x.a[i] + y.a[i];
+    return r;
+}
+template <typename VT, int V>
+__device__ __forceinline__ vv<VT, V> vv_shfl(const vv<VT, V>& x, int src) {
+    vv<VT, V> r;
+#pragma unroll
+    for (int i = 0; i < V; ++i)
+        r.a[i] = __shfl_sync(kFull, x.a[i], src);
+    return r;
+}
+
+// Read-only gather of V consecutive values (16-byte vector loads where V * sizeof(VT) allows), kept in L1
+// and L2 like the SpMV's x gathers.
+template <typename VT, int V>
+__device__ __forceinline__ vv<VT, V> ldg_vec(const VT* p, uint64_t pol) {
+    vv<VT, V> r;
+    if constexpr (V == 1) {
+        r.a[0] = ldg_x(p, pol);
+    } else if constexpr (sizeof(VT) == 4 && V == 2) {
+        asm("ld.global.nc.L1::evict_last.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
+            : "=f"(r.a[0]), "=f"(r.a[1])
+            : "l"(p), "l"(pol));
+    } else if constexpr (sizeof(VT) == 4 && V == 4) {
+        asm("ld.global.nc.L1::evict_last.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+            : "=f"(r.a[0]), "=f"(r.a[1]), "=f"(r.a[2]), "=f"(r.a[3])
+            : "l"(p), "l"(pol));
+    } else {
+#pragma unroll
+        for (int h = 0; h < V; h += 2)
+            asm("ld.global.nc.L1::evict_last.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+                : "=d"(r.a[h]), "=d"(r.a[h + 1])
+                : "l"(p + h), "l"(pol));
+    }
+    return r;
+}
+
+template <typename VT, int V>
+__device__ __forceinline__ void st_vec(VT* p, const vv<VT, V>& v) {
+    if constexpr (V == 1) {
+        p[0] = v.a[0];
+    } else if constexpr (sizeof(VT) == 4 && V == 2) {
+        *reinterpret_cast<float2*>(p) = make_float2(v.a[0], v.a[1]);
+    } else if constexpr (sizeof(VT) == 4 && V == 4) {
+        *reinterpret_cast<float4*>(p) = make_float4(v.a[0], v.a[1], v.a[2], v.a[3]);
+    } else {
+#pragma unroll
+        for (int h = 0; h < V; h += 2)
+            *reinterpret_cast<double2*>(p + h) = make_double2(v.a[h], v.a[h + 1]);
+    }
+}
+
+// Y = A X.  KP = k rounded up to 8, 16 or 32; each lane holds V consecutive right-hand sides, so a lane
+// group has LG = KP / V lanes and a warp NG = 32 / LG groups; group g walks tile columns [g LG, (g+1) LG).
+template <typename VT, int KP, int V, int WPC, int STAGES, bool DOT>
 __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
     using G = mm_geom<VT>;
-    constexpr int NG = 32 / KP;  // lane groups per warp
+    using W = vv<VT, V>;
+    constexpr int LG = KP / V;   // lanes per group
+    constexpr int NG = 32 / LG;  // lane groups per warp
+    // rows gathered together (registers: RB x V values of x in flight per lane)
+    constexpr int RB = (V * sizeof(VT) <= 8) ? kSigma : kSigma * 8 / (int)(V * sizeof(VT));
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint32_t s_last, s_cta, s_epoch;
     __shared__ double s_dot[WPC][32];
@@ -125,8 +211,8 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
     if (p.halt && *reinterpret_cast<volatile const uint32_t*>(p.halt))
         return;
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const unsigned g = lane / KP, j = lane % KP;
-    const bool active = j < p.k;
+    const unsigned g = lane / LG, j = lane % LG;
+    const bool active = j * V < p.k;  // the host sends V > 1 only when k is a multiple of V
     if (threadIdx.x == 0) {
         s_cta = atomicAdd(&p.words[2], 1u);
         s_epoch = *reinterpret_cast<volatile const uint32_t*>(&p.words[3]) + 1u;
@@ -146,18 +232,25 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
     const uint64_t t_end = min(p.T, t_begin + p.tpw);
     const uint64_t pol_keep = policy_evict_last();
 
-    double dot_acc = 0.0;
-    VT tdot = VT(0);  // this tile's share of the dot, folded into dot_acc once per tile
+    double dot_acc[V];
+#pragma unroll
+    for (int i = 0; i < V; ++i)
+        dot_acc[i] = 0.0;
+    W tdot = vv_zero<VT, V>();  // this tile's share of the dot, folded into dot_acc once per tile
     bool open = false, cal_valid = false;
-    VT carry = VT(0), cal = VT(0);
+    W carry = vv_zero<VT, V>(), cal = vv_zero<VT, V>();
     uint32_t carry_row = 0, cal_row = 0;
 
     // k-wide row write by the lanes of one group (`mine`), with its share of the dot
-    auto put_row = [&](bool mine, uint32_t row, VT val) {
+    auto put_row = [&](bool mine, uint32_t row, const W& val) {
         if (mine && active) {
-            st_keep(p.Y + (uint64_t)row * p.ldy + j, val, pol_keep);
-            if constexpr (DOT)
-                tdot = fma(val, ldg_x(p.X + (uint64_t)row * p.ldx + j, pol_keep), tdot);
+            st_vec<VT, V>(p.Y + (uint64_t)row * p.ldy + j * V, val);
+            if constexpr (DOT) {
+                const W xr = ldg_vec<VT, V>(p.X + (uint64_t)row * p.ldx + j * V, pol_keep);
+#pragma unroll
+                for (int i = 0; i < V; ++i)
+                    tdot.a[i] = fma(val.a[i], xr.a[i], tdot.a[i]);
+            }
         }
     };
 
@@ -204,76 +297,82 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
             };
             const bool capped = ((sd[0] >> (G::F.yb + G::F.sb)) & 1u) != 0;
 
-            // ---- this group's elements: tile columns [c0, c0 + KP) ----
-            const uint32_t c0 = g * KP;
+            // ---- this group's elements: tile columns [c0, c0 + LG) ----
+            const uint32_t c0 = g * LG;
             // segments are numbered by the row starts after tile element 0 (y_offset counts element 0 once)
             uint32_t seg = (c0 == 0) ? 0u : ((sd[c0] & G::YMASK) - 1u);
-            VT acc = VT(0), head = VT(0);
+            W acc = vv_zero<VT, V>(), head = vv_zero<VT, V>();
             bool hs = false;
-            // gathers of tile column c into x (X[col, j] for its 16 elements)
-            auto gather = [&](uint32_t c, VT (&x)[kSigma]) {
+            // gathers of rows [r0, r0 + RB) of tile column c (X[col, jV .. jV+V) per element)
+            auto gather = [&](uint32_t c, int r0, W (&x)[RB]) {
                 uint32_t ci[kSigma];
                 stage_cols(st + G::VBYTES, c, ci);
 #pragma unroll
-                for (int r = 0; r < kSigma; ++r)
-                    x[r] = active ? ldg_x(p.X + (uint64_t)ci[r] * p.ldx + j, pol_keep) : VT(0);
+                for (int r = 0; r < RB; ++r)
+                    x[r] = active ? ldg_vec<VT, V>(p.X + (uint64_t)ci[r0 + r] * p.ldx + j * V, pol_keep)
+                                  : vv_zero<VT, V>();
             };
-            // the 16 elements of tile column c, in CSR order, with their gathered x
-            auto walk = [&](uint32_t c, const VT (&x)[kSigma]) {
+            // rows [r0, r0 + RB) of tile column c, in CSR order, with their gathered x
+            auto walk = [&](uint32_t c, int r0, const W (&x)[RB]) {
                 uint32_t fl = (sd[c] >> (G::F.yb + G::F.sb)) & 0xFFFFu;
                 if (c == 0)
                     fl &= ~1u;  // element 0 opens segment 0 without closing anything
                 VT v[kSigma];
                 stage_vals<VT>(st, c, v);
 #pragma unroll
-                for (int r = 0; r < kSigma; ++r) {
-                    if ((fl >> r) & 1u) {
+                for (int r = 0; r < RB; ++r) {
+                    if ((fl >> (r0 + r)) & 1u) {
                         if (hs)
                             put_row(true, row_of(seg), acc);  // a row that began in this group's range
                         else
                             head = acc;
                         hs = true;
                         ++seg;
-                        acc = VT(0);
+                        acc = vv_zero<VT, V>();
                     }
-                    acc = fma(v[r], x[r], acc);
+#pragma unroll
+                    for (int q = 0; q < V; ++q)
+                        acc.a[q] = fma(v[r0 + r], x[r].a[q], acc.a[q]);
                 }
             };
-            if constexpr (sizeof(VT) == 4) {
-                // f32: the next column's gathers are in flight while this one accumulates
-                VT xa[kSigma], xb[kSigma];
-                gather(c0, xa);
+            if constexpr (sizeof(VT) == 4 && V == 1) {
+                // f32, one value per lane: the next column's gathers are in flight while this one accumulates
+                W xa[RB], xb[RB];
+                gather(c0, 0, xa);
 #pragma unroll 1
-                for (uint32_t cc = 0; cc < (uint32_t)KP; cc += 2) {
-                    gather(c0 + cc + 1, xb);
-                    walk(c0 + cc, xa);
-                    if (cc + 2 < (uint32_t)KP)
-                        gather(c0 + cc + 2, xa);
-                    walk(c0 + cc + 1, xb);
+                for (uint32_t cc = 0; cc < (uint32_t)LG; cc += 2) {
+                    gather(c0 + cc + 1, 0, xb);
+                    walk(c0 + cc, 0, xa);
+                    if (cc + 2 < (uint32_t)LG)
+                        gather(c0 + cc + 2, 0, xa);
+                    walk(c0 + cc + 1, 0, xb);
                 }
             } else {
 #pragma unroll 1
-                for (uint32_t cc = 0; cc < (uint32_t)KP; ++cc) {
-                    VT xv[kSigma];
-                    gather(c0 + cc, xv);
-                    walk(c0 + cc, xv);
+                for (uint32_t cc = 0; cc < (uint32_t)LG; ++cc) {
+#pragma unroll
+                    for (int r0 = 0; r0 < kSigma; r0 += RB) {
+                        W xv[RB];
+                        gather(c0 + cc, r0, xv);
+                        walk(c0 + cc, r0, xv);
+                    }
                 }
             }
             if (!hs)
                 head = acc;
 
             // ---- join the groups in order: rows spanning groups, the tile's head and open segments ----
-            VT open_v = VT(0), H = VT(0);
+            W open_v = vv_zero<VT, V>(), H = vv_zero<VT, V>();
             uint32_t open_seg = 0;
             bool closed0 = false;
 #pragma unroll
             for (int gg = 0; gg < NG; ++gg) {
-                const int src = gg * KP + (int)j;
+                const int src = gg * LG + (int)j;
                 const uint32_t ghs = __shfl_sync(kFull, hs ? 1u : 0u, src);
-                const VT ghd = __shfl_sync(kFull, head, src);
-                const VT gtl = __shfl_sync(kFull, acc, src);
+                const W ghd = vv_shfl<VT, V>(head, src);
+                const W gtl = vv_shfl<VT, V>(acc, src);
                 const uint32_t gseg = __shfl_sync(kFull, seg, src);
-                open_v += ghd;
+                vv_add<VT, V>(open_v, ghd);
                 if (ghs) {
                     if (open_seg == 0) {
                         H = open_v;
@@ -288,7 +387,7 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
             if (!closed0)
                 H = open_v;
             const uint32_t K = open_seg + 1;
-            const VT Lt = open_v;
+            const W Lt = open_v;
             const uint32_t row_last = (K == 1) ? row_start : row_of(open_seg);
 
             // ---- in-order carry chain over the warp's tiles (per right-hand side, same in every group) ----
@@ -300,9 +399,9 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
                     carry = H;
                     carry_row = row_start;
                 } else if (open) {
-                    carry += H;
+                    vv_add<VT, V>(carry, H);
                 } else {
-                    cal += H;
+                    vv_add<VT, V>(cal, H);
                     cal_row = row_start;
                     cal_valid = true;
                 }
@@ -312,9 +411,9 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
                         put_row(g == 0, carry_row, carry);
                     put_row(g == 0, row_start, H);
                 } else if (open) {
-                    put_row(g == 0, row_start, carry + H);
+                    put_row(g == 0, row_start, vv_sum<VT, V>(carry, H));
                 } else {
-                    cal += H;
+                    vv_add<VT, V>(cal, H);
                     cal_row = row_start;
                     cal_valid = true;
                 }
@@ -323,8 +422,11 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
                 carry_row = row_last;
             }
             if constexpr (DOT) {
-                dot_acc += (double)tdot;
-                tdot = VT(0);
+#pragma unroll
+                for (int q = 0; q < V; ++q) {
+                    dot_acc[q] += (double)tdot.a[q];
+                    tdot.a[q] = VT(0);
+                }
             }
             __syncwarp();
             if (lane == 0 && t + STAGES < t_end) {
@@ -352,7 +454,10 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
         else if (through && cont_after)
             kind = kFragThrough;
         if (kind != kFragNone && g == 0) {
-            p.frag_val[(uint64_t)run * 32 + j] = (double)(kind == kFragCarry ? carry : cal);
+            const W& fv = kind == kFragCarry ? carry : cal;
+#pragma unroll
+            for (int q = 0; q < V; ++q)
+                p.frag_val[(uint64_t)run * 32 + j * V + q] = (double)fv.a[q];
             if (j == 0)
                 p.frag_row[run] = kind == kFragCarry ? carry_row : cal_row;
             __threadfence();
@@ -379,22 +484,35 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
                 }
             }
             first = __shfl_sync(kFull, first, 0);
-            VT v = VT(0);
-            if (first < run) {
-                v = (VT)__ldcg(&p.frag_val[(uint64_t)first * 32 + j]);
-                for (uint32_t k2 = first + 1; k2 < run; ++k2)
-                    v += (VT)__ldcg(&p.frag_val[(uint64_t)k2 * 32 + j]);
+            W v = vv_zero<VT, V>();
+            if (first < run && g == 0) {
+#pragma unroll
+                for (int q = 0; q < V; ++q) {
+                    VT a = (VT)__ldcg(&p.frag_val[(uint64_t)first * 32 + j * V + q]);
+                    for (uint32_t k2 = first + 1; k2 < run; ++k2)
+                        a += (VT)__ldcg(&p.frag_val[(uint64_t)k2 * 32 + j * V + q]);
+                    v.a[q] = a;
+                }
             }
-            put_row(g == 0, cal_row, v + cal);
+            put_row(g == 0, cal_row, vv_sum<VT, V>(v, cal));
         }
     }
     if constexpr (DOT) {
-        dot_acc += (double)tdot;
-        // sum over the groups (same right-hand side j), then per CTA in warp order
 #pragma unroll
-        for (int o = KP; o < 32; o <<= 1)
-            dot_acc += __shfl_xor_sync(kFull, dot_acc, o);
-        s_dot[warp][lane] = dot_acc;
+        for (int q = 0; q < V; ++q) {
+            dot_acc[q] += (double)tdot.a[q];
+            // sum over the groups (same right-hand sides), then per CTA in warp order
+#pragma unroll
+            for (int o = LG; o < 32; o <<= 1)
+                dot_acc[q] += __shfl_xor_sync(kFull, dot_acc[q], o);
+        }
+        s_dot[warp][lane] = 0.0;
+        __syncwarp();
+        if (g == 0) {
+#pragma unroll
+            for (int q = 0; q < V; ++q)
+                s_dot[warp][j * V + q] = dot_acc[q];
+        }
     }
 
     // ---- completion ticket; the last CTA computes the CSR tail and the per-column dots ----
@@ -492,13 +610,13 @@ constexpr size_t mm_smem() {
     return 128 * ((WPC * STAGES * 8 + 127) / 128) + (size_t)WPC * STAGES * mm_geom<VT>::STAGE;
 }
 
-template <typename VT, int KP, int WPC, int STAGES, bool DOT>
+template <typename VT, int KP, int V, int WPC, int STAGES, bool DOT>
 cudaError_t mm_attr() {
-    return cudaFuncSetAttribute(k_spmm<VT, KP, WPC, STAGES, DOT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(k_spmm<VT, KP, V, WPC, STAGES, DOT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)mm_smem<VT, WPC, STAGES>());
 }
 
-template <typename VT, int KP, int WPC, int STAGES, bool DOT>
+template <typename VT, int KP, int V, int WPC, int STAGES, bool DOT>
 int mm_launch(const dimgpu_csr5* m, const VT* vals, const spmm_args& a, const spmm_scratch& sc, cudaStream_t st) {
     const spmv_plan pl = make_spmv_plan(m->tile_count, device_sm_count(m->device), WPC);
     if (pl.nwarps > sc.nslots)
@@ -536,20 +654,33 @@ int mm_launch(const dimgpu_csr5* m, const VT* vals, const spmm_args& a, const sp
     p.mask = a.mask;
     p.mask_sel = a.mask_sel;
     p.halt = a.halt;
-    k_spmm<VT, KP, WPC, STAGES, DOT><<<pl.grid, WPC * 32, mm_smem<VT, WPC, STAGES>(), st>>>(p);
+    k_spmm<VT, KP, V, WPC, STAGES, DOT><<<pl.grid, WPC * 32, mm_smem<VT, WPC, STAGES>(), st>>>(p);
     DG_CUDA(cudaGetLastError());
     return DIMGPU_OK;
 }
 
-template <typename VT, int KP, bool DOT>
+template <typename VT, int KP, int V, bool DOT>
 int mm_dispatch_kp(const dimgpu_csr5* m, const VT* vals, const spmm_args& a, const spmm_scratch& sc, int shape,
                    cudaStream_t st) {
     switch (shape) {
     case 0:
-        return mm_launch<VT, KP, 8, 3, DOT>(m, vals, a, sc, st);
+        return mm_launch<VT, KP, V, 8, 3, DOT>(m, vals, a, sc, st);
     default:
-        return mm_launch<VT, KP, 16, 2, DOT>(m, vals, a, sc, st);
+        return mm_launch<VT, KP, V, 16, 2, DOT>(m, vals, a, sc, st);
     }
+}
+
+// Values per lane: KP / 8 (four lane groups of eight lanes) when k and the layout allow vector accesses
+// (k and both leading dimensions multiples of it, X and Y aligned to it); one value per lane otherwise.
+template <typename VT>
+int lanes_vec(const spmm_args& a, int kp) {
+    const int v = kp / 8;
+    if (v <= 1)
+        return 1;
+    const uintptr_t align = (uintptr_t)v * sizeof(VT);
+    const bool ok = a.k % v == 0 && a.ldx % v == 0 && a.ldy % v == 0 &&
+                    reinterpret_cast<uintptr_t>(a.X) % align == 0 && reinterpret_cast<uintptr_t>(a.Y) % align == 0;
+    return ok ? v : 1;
 }
 
 // Lane-group width for k right-hand sides.
@@ -558,25 +689,42 @@ inline int kp_for(uint32_t k) { return k <= 8 ? 8 : (k <= 16 ? 16 : 32); }
 template <typename VT, bool DOT>
 int mm_dispatch(const dimgpu_csr5* m, const VT* vals, const spmm_args& a, const spmm_scratch& sc, int shape,
                 cudaStream_t st) {
-    switch (kp_for(a.k)) {
+    const int kp = kp_for(a.k);
+    if constexpr (sizeof(VT) == 4) {
+        // f32 is issue-bound: share the per-element work over four elements with vector lanes
+        const int v = lanes_vec<VT>(a, kp);
+        if (kp == 16 && v == 2)
+            return mm_dispatch_kp<VT, 16, 2, DOT>(m, vals, a, sc, shape, st);
+        if (kp == 32 && v == 4)
+            return mm_dispatch_kp<VT, 32, 4, DOT>(m, vals, a, sc, shape, st);
+    }
+    // FP64 is bound by the FP64 pipe (the same DFMA count either way): one value per lane
+    switch (kp) {
     case 8:
-        return mm_dispatch_kp<VT, 8, DOT>(m, vals, a, sc, shape, st);
+        return mm_dispatch_kp<VT, 8, 1, DOT>(m, vals, a, sc, shape, st);
     case 16:
-        return mm_dispatch_kp<VT, 16, DOT>(m, vals, a, sc, shape, st);
+        return mm_dispatch_kp<VT, 16, 1, DOT>(m, vals, a, sc, shape, st);
     default:
-        return mm_dispatch_kp<VT, 32, DOT>(m, vals, a, sc, shape, st);
+        return mm_dispatch_kp<VT, 32, 1, DOT>(m, vals, a, sc, shape, st);
     }
 }
 
 template <typename VT, bool DOT>
 cudaError_t mm_attrs() {
     cudaError_t e;
-    if ((e = mm_attr<VT, 8, 8, 3, DOT>()) != cudaSuccess) return e;
-    if ((e = mm_attr<VT, 8, 16, 2, DOT>()) != cudaSuccess) return e;
-    if ((e = mm_attr<VT, 16, 8, 3, DOT>()) != cudaSuccess) return e;
-    if ((e = mm_attr<VT, 16, 16, 2, DOT>()) != cudaSuccess) return e;
-    if ((e = mm_attr<VT, 32, 8, 3, DOT>()) != cudaSuccess) return e;
-    return mm_attr<VT, 32, 16, 2, DOT>();
+    if ((e = mm_attr<VT, 8, 1, 8, 3, DOT>()) != cudaSuccess) return e;
+    if ((e = mm_attr<VT, 8, 1, 16, 2, DOT>()) != cudaSuccess) return e;
+    if ((e = mm_attr<VT, 16, 1, 8, 3, DOT>()) != cudaSuccess) return e;
+    if ((e = mm_attr<VT, 16, 1, 16, 2, DOT>()) != cudaSuccess) return e;
+    if ((e = mm_attr<VT, 32, 1, 8, 3, DOT>()) != cudaSuccess) return e;
+    if ((e = mm_attr<VT, 32, 1, 16, 2, DOT>()) != cudaSuccess) return e;
+    if constexpr (sizeof(VT) == 4) {
+        if ((e = mm_attr<VT, 16, 2, 8, 3, DOT>()) != cudaSuccess) return e;
+        if ((e = mm_attr<VT, 16, 2, 16, 2, DOT>()) != cudaSuccess) return e;
+        if ((e = mm_attr<VT, 32, 4, 8, 3, DOT>()) != cudaSuccess) return e;
+        if ((e = mm_attr<VT, 32, 4, 16, 2, DOT>()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace
