@@ -38,7 +38,7 @@ class CGSolver:
     host-driven loop of kernels."""
 
     def __init__(self, A: csr5, tol: float = 1e-10, max_it: int = 100000, precision: str = "fp64",
-                 use_graph: bool = True, reliable_delta: float = 0.1, stream=None, engine: str = "auto"):
+                 use_graph: bool = True, reliable_delta: float = 0.03, stream=None, engine: str = "auto"):
         if precision not in _PREC:
             raise ValueError(f"precision must be one of {sorted(_PREC)}")
         if engine not in _ENGINE:

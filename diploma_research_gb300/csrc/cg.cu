@@ -723,7 +723,7 @@ int dimgpu_cg_create(const dimgpu_csr5* m, const dimgpu_cg_params* params, void*
     s->m = m;
     s->params = *params;
     if (s->params.reliable_delta <= 0 || s->params.reliable_delta >= 1)
-        s->params.reliable_delta = 0.1;
+        s->params.reliable_delta = 0.03;
     s->n = m->rows;
     const int sms = device_sm_count(m->device);
     // two resident blocks per SM (fewer for short vectors)
