@@ -48,13 +48,13 @@ struct spmm_params {
     uint64_t T;
     uint32_t rows;
     uint32_t tail_start;
-    uint64_t tpw;
-    uint32_t nwarps;
+    uint64_t chunk;      // tiles per chunk
+    uint32_t nchunks;
     const uint32_t* empty_rows;
     uint32_t n_empty;
-    double* frag_val;    // [nwarps * 32] the k-vector fragment a run publishes for a later run
-    uint32_t* frag_row;  // [nwarps]
-    uint32_t* flag;      // [nwarps] (epoch << 2) | fragment kind
+    double* frag_val;    // [nchunks * 32] the k-vector fragment a chunk publishes for a later chunk
+    uint32_t* frag_row;  // [nchunks]
+    uint32_t* flag;      // [nchunks] (epoch << 2) | fragment kind
     double* cta_part;    // [grid * 32] per-CTA partials of the per-column dots
     uint32_t* words;     // [0] completion ticket, [2] run counter, [3] launch epoch
     uint32_t* status;
@@ -69,6 +69,7 @@ struct spmm_params {
 
 constexpr int kSigma = 16;
 constexpr uint32_t kTS = kSigma * 32;
+constexpr int kSpmmRounds = 4;  // chunks per warp
 
 template <typename VT>
 struct mm_geom {
@@ -205,7 +206,7 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
     // rows gathered together (registers: RB x V values of x in flight per lane)
     constexpr int RB = (V * sizeof(VT) <= 8) ? kSigma : kSigma * 8 / (int)(V * sizeof(VT));
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ uint32_t s_last, s_cta, s_epoch;
+    __shared__ uint32_t s_last, s_epoch;
     __shared__ double s_dot[WPC][32];
 
     if (p.halt && *reinterpret_cast<volatile const uint32_t*>(p.halt))
@@ -213,10 +214,8 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const unsigned g = lane / LG, j = lane % LG;
     const bool active = j * V < p.k;  // the host sends V > 1 only when k is a multiple of V
-    if (threadIdx.x == 0) {
-        s_cta = atomicAdd(&p.words[2], 1u);
+    if (threadIdx.x == 0)
         s_epoch = *reinterpret_cast<volatile const uint32_t*>(&p.words[3]) + 1u;
-    }
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem) + warp * STAGES;
     unsigned char* ring = smem + 128 * ((WPC * STAGES * 8 + 127) / 128) + (size_t)warp * STAGES * G::STAGE;
 
@@ -225,11 +224,13 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
         if (lane < p.k)
             p.Y[(uint64_t)p.empty_rows[i] * p.ldy + lane] = VT(0);
     __syncthreads();
-    const uint32_t cta = s_cta;
     const uint32_t epoch = (s_epoch & 0x3fffffffu) ? (s_epoch & 0x3fffffffu) : 1u;
-    const uint32_t run = cta * WPC + warp;
-    const uint64_t t_begin = min(p.T, (uint64_t)run * p.tpw);
-    const uint64_t t_end = min(p.T, t_begin + p.tpw);
+    // Chunks of p.chunk consecutive tiles are dealt to the warps round-robin (chunk c to warp c mod nw),
+    // so at any moment the warps work on one band of neighbouring tiles and the rows of X that several
+    // tiles gather are still in L2 for all of them.  The launch is cooperative (every CTA resident), so a
+    // chunk may wait for the previous chunk's fragment whichever warp holds it.
+    const uint32_t gw = blockIdx.x * WPC + warp, nw = gridDim.x * WPC;
+    const uint64_t C = p.chunk;
     const uint64_t pol_keep = policy_evict_last();
 
     double dot_acc[V];
@@ -254,7 +255,7 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
         }
     };
 
-    if (t_begin < t_end) {
+    {
         const uint64_t pol = policy_evict_first();
         if (lane == 0) {
             for (int s = 0; s < STAGES; ++s)
@@ -262,239 +263,264 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
             fence_mbar_init();
         }
         __syncwarp();
-        auto issue = [&](int s, uint64_t t) {
+        // this warp's j-th tile: chunk gw + (j / C) nw, tile j mod C of it (or T: no such tile)
+        auto seq_tile = [&](uint64_t jt) -> uint64_t {
+            const uint64_t c = gw + (jt / C) * (uint64_t)nw;
+            if (c >= p.nchunks)
+                return p.T;
+            const uint64_t t = c * C + jt % C;
+            return t < p.T ? t : p.T;
+        };
+        auto issue = [&](uint64_t q, uint64_t t) {  // ring position q <- tile t (lane 0)
+            const int s = (int)(q % STAGES);
             unsigned char* st = ring + (size_t)s * G::STAGE;
             mbar_arrive_expect_tx(&bars[s], G::STAGE);
             bulk_g2s(st, p.vals + t * kTS, G::VBYTES, &bars[s], pol);
             bulk_g2s(st + G::VBYTES, p.col + t * kTS, G::CBYTES, &bars[s], pol);
             bulk_g2s(st + G::VBYTES + G::CBYTES, p.desc + t * 32, G::DBYTES, &bars[s], pol);
         };
-        if (lane == 0)
-            for (int s = 0; s < STAGES && t_begin + s < t_end; ++s)
-                issue(s, t_begin + s);
-
-        uint32_t raw_cur = __ldg(&p.tile_ptr[t_begin]);
-        uint32_t raw_next = __ldg(&p.tile_ptr[t_begin + 1]);
-        uint64_t i = 0;
+        uint64_t qi = 0;  // ring positions issued (uniform across the lanes; lane 0 issues)
+        for (int j0 = 0; j0 < STAGES; ++j0) {
+            const uint64_t t = seq_tile(j0);
+            if (t >= p.T)
+                break;
+            if (lane == 0)
+                issue(j0, t);
+            ++qi;
+        }
+        uint64_t q = 0;  // ring position of the tile being consumed
         bool failed = false;
-        for (uint64_t t = t_begin; t < t_end; ++t, ++i) {
-            const int s = (int)(i % STAGES);
-            const uint32_t par = (uint32_t)((i / STAGES) & 1);
-            const uint32_t raw = raw_cur;
-            const uint32_t row_start = raw & ~kDirty;
-            raw_cur = raw_next;
-            raw_next = (t + 2 <= p.T) ? __ldg(&p.tile_ptr[t + 2]) : 0u;
-            if (!mbar_wait_bounded(&bars[s], par, p.status)) {
-                failed = true;
+        for (uint64_t c = gw; c < p.nchunks && !failed; c += nw) {
+            const uint64_t cb = c * C, ce = min(p.T, cb + C);
+            open = false;
+            cal_valid = false;
+            carry = vv_zero<VT, V>();
+            cal = vv_zero<VT, V>();
+            uint32_t raw_cur = __ldg(&p.tile_ptr[cb]);
+            uint32_t raw_next = __ldg(&p.tile_ptr[cb + 1]);
+            for (uint64_t t = cb; t < ce; ++t, ++q) {
+                const int s = (int)(q % STAGES);
+                const uint32_t par = (uint32_t)((q / STAGES) & 1);
+                const uint32_t raw = raw_cur;
+                const uint32_t row_start = raw & ~kDirty;
+                raw_cur = raw_next;
+                raw_next = (t + 2 <= p.T) ? __ldg(&p.tile_ptr[t + 2]) : 0u;
+                if (!mbar_wait_bounded(&bars[s], par, p.status)) {
+                    failed = true;
+                    break;
+                }
+                const unsigned char* st = ring + (size_t)s * G::STAGE;
+                const uint32_t* sd = reinterpret_cast<const uint32_t*>(st + G::VBYTES + G::CBYTES);
+                const bool dirty = (raw & kDirty) != 0;
+                const uint32_t optr = dirty ? __ldg(&p.tdo_ptr[t]) : 0u;
+                auto row_of = [&](uint32_t idx) -> uint32_t {
+                    return row_start + (dirty ? __ldg(&p.tdo[optr + idx]) : idx);
+                };
+                const bool capped = ((sd[0] >> (G::F.yb + G::F.sb)) & 1u) != 0;
+
+                // ---- this group's elements: tile columns [c0, c0 + LG) ----
+                const uint32_t c0 = g * LG;
+                // segments are numbered by the row starts after tile element 0 (y_offset counts element 0 once)
+                uint32_t seg = (c0 == 0) ? 0u : ((sd[c0] & G::YMASK) - 1u);
+                W acc = vv_zero<VT, V>(), head = vv_zero<VT, V>();
+                bool hs = false;
+                // gathers of rows [r0, r0 + RB) of tile column c (X[col, jV .. jV+V) per element)
+                auto gather = [&](uint32_t c, int r0, W (&x)[RB]) {
+                    uint32_t ci[kSigma];
+                    stage_cols(st + G::VBYTES, c, ci);
+    #pragma unroll
+                    for (int r = 0; r < RB; ++r)
+                        x[r] = active ? ldg_vec<VT, V>(p.X + (uint64_t)ci[r0 + r] * p.ldx + j * V, pol_keep)
+                                      : vv_zero<VT, V>();
+                };
+                // rows [r0, r0 + RB) of tile column c, in CSR order, with their gathered x
+                auto walk = [&](uint32_t c, int r0, const W (&x)[RB]) {
+                    uint32_t fl = (sd[c] >> (G::F.yb + G::F.sb)) & 0xFFFFu;
+                    if (c == 0)
+                        fl &= ~1u;  // element 0 opens segment 0 without closing anything
+                    VT v[kSigma];
+                    stage_vals<VT>(st, c, v);
+    #pragma unroll
+                    for (int r = 0; r < RB; ++r) {
+                        if ((fl >> (r0 + r)) & 1u) {
+                            if (hs)
+                                put_row(true, row_of(seg), acc);  // a row that began in this group's range
+                            else
+                                head = acc;
+                            hs = true;
+                            ++seg;
+                            acc = vv_zero<VT, V>();
+                        }
+    #pragma unroll
+                        for (int q = 0; q < V; ++q)
+                            acc.a[q] = fma(v[r0 + r], x[r].a[q], acc.a[q]);
+                    }
+                };
+                if constexpr (sizeof(VT) == 4 && V == 1) {
+                    // f32, one value per lane: the next column's gathers are in flight while this one accumulates
+                    W xa[RB], xb[RB];
+                    gather(c0, 0, xa);
+    #pragma unroll 1
+                    for (uint32_t cc = 0; cc < (uint32_t)LG; cc += 2) {
+                        gather(c0 + cc + 1, 0, xb);
+                        walk(c0 + cc, 0, xa);
+                        if (cc + 2 < (uint32_t)LG)
+                            gather(c0 + cc + 2, 0, xa);
+                        walk(c0 + cc + 1, 0, xb);
+                    }
+                } else {
+    #pragma unroll 1
+                    for (uint32_t cc = 0; cc < (uint32_t)LG; ++cc) {
+    #pragma unroll
+                        for (int r0 = 0; r0 < kSigma; r0 += RB) {
+                            W xv[RB];
+                            gather(c0 + cc, r0, xv);
+                            walk(c0 + cc, r0, xv);
+                        }
+                    }
+                }
+                if (!hs)
+                    head = acc;
+
+                // ---- join the groups in order: rows spanning groups, the tile's head and open segments ----
+                W open_v = vv_zero<VT, V>(), H = vv_zero<VT, V>();
+                uint32_t open_seg = 0;
+                bool closed0 = false;
+    #pragma unroll
+                for (int gg = 0; gg < NG; ++gg) {
+                    const int src = gg * LG + (int)j;
+                    const uint32_t ghs = __shfl_sync(kFull, hs ? 1u : 0u, src);
+                    const W ghd = vv_shfl<VT, V>(head, src);
+                    const W gtl = vv_shfl<VT, V>(acc, src);
+                    const uint32_t gseg = __shfl_sync(kFull, seg, src);
+                    vv_add<VT, V>(open_v, ghd);
+                    if (ghs) {
+                        if (open_seg == 0) {
+                            H = open_v;
+                            closed0 = true;
+                        } else {
+                            put_row(g == (unsigned)gg, row_of(open_seg), open_v);
+                        }
+                        open_v = gtl;
+                        open_seg = gseg;
+                    }
+                }
+                if (!closed0)
+                    H = open_v;
+                const uint32_t K = open_seg + 1;
+                const W Lt = open_v;
+                const uint32_t row_last = (K == 1) ? row_start : row_of(open_seg);
+
+                // ---- in-order carry chain over the warp's tiles (per right-hand side, same in every group) ----
+                if (K == 1) {
+                    if (capped) {
+                        if (open)
+                            put_row(g == 0, carry_row, carry);
+                        open = true;
+                        carry = H;
+                        carry_row = row_start;
+                    } else if (open) {
+                        vv_add<VT, V>(carry, H);
+                    } else {
+                        vv_add<VT, V>(cal, H);
+                        cal_row = row_start;
+                        cal_valid = true;
+                    }
+                } else {
+                    if (capped) {
+                        if (open)
+                            put_row(g == 0, carry_row, carry);
+                        put_row(g == 0, row_start, H);
+                    } else if (open) {
+                        put_row(g == 0, row_start, vv_sum<VT, V>(carry, H));
+                    } else {
+                        vv_add<VT, V>(cal, H);
+                        cal_row = row_start;
+                        cal_valid = true;
+                    }
+                    open = true;
+                    carry = Lt;
+                    carry_row = row_last;
+                }
+                if constexpr (DOT) {
+    #pragma unroll
+                    for (int q = 0; q < V; ++q) {
+                        dot_acc[q] += (double)tdot.a[q];
+                        tdot.a[q] = VT(0);
+                    }
+                }
+                __syncwarp();
+                // refill this slot with the warp's tile STAGES positions ahead (this chunk or its next one)
+                const uint64_t tn = seq_tile(q + STAGES);
+                if (tn < p.T) {
+                    if (lane == 0) {
+                        fence_proxy_async_smem();
+                        issue(q + STAGES, tn);
+                    }
+                    ++qi;
+                }
+            }
+            if (failed) {
+                for (uint64_t q2 = q; q2 < qi; ++q2)
+                    (void)mbar_wait_bounded(&bars[q2 % STAGES], (uint32_t)((q2 / STAGES) & 1), p.status);
                 break;
             }
-            const unsigned char* st = ring + (size_t)s * G::STAGE;
-            const uint32_t* sd = reinterpret_cast<const uint32_t*>(st + G::VBYTES + G::CBYTES);
-            const bool dirty = (raw & kDirty) != 0;
-            const uint32_t optr = dirty ? __ldg(&p.tdo_ptr[t]) : 0u;
-            auto row_of = [&](uint32_t idx) -> uint32_t {
-                return row_start + (dirty ? __ldg(&p.tdo[optr + idx]) : idx);
-            };
-            const bool capped = ((sd[0] >> (G::F.yb + G::F.sb)) & 1u) != 0;
 
-            // ---- this group's elements: tile columns [c0, c0 + LG) ----
-            const uint32_t c0 = g * LG;
-            // segments are numbered by the row starts after tile element 0 (y_offset counts element 0 once)
-            uint32_t seg = (c0 == 0) ? 0u : ((sd[c0] & G::YMASK) - 1u);
-            W acc = vv_zero<VT, V>(), head = vv_zero<VT, V>();
-            bool hs = false;
-            // gathers of rows [r0, r0 + RB) of tile column c (X[col, jV .. jV+V) per element)
-            auto gather = [&](uint32_t c, int r0, W (&x)[RB]) {
-                uint32_t ci[kSigma];
-                stage_cols(st + G::VBYTES, c, ci);
-#pragma unroll
-                for (int r = 0; r < RB; ++r)
-                    x[r] = active ? ldg_vec<VT, V>(p.X + (uint64_t)ci[r0 + r] * p.ldx + j * V, pol_keep)
-                                  : vv_zero<VT, V>();
-            };
-            // rows [r0, r0 + RB) of tile column c, in CSR order, with their gathered x
-            auto walk = [&](uint32_t c, int r0, const W (&x)[RB]) {
-                uint32_t fl = (sd[c] >> (G::F.yb + G::F.sb)) & 0xFFFFu;
-                if (c == 0)
-                    fl &= ~1u;  // element 0 opens segment 0 without closing anything
-                VT v[kSigma];
-                stage_vals<VT>(st, c, v);
-#pragma unroll
-                for (int r = 0; r < RB; ++r) {
-                    if ((fl >> (r0 + r)) & 1u) {
-                        if (hs)
-                            put_row(true, row_of(seg), acc);  // a row that began in this group's range
-                        else
-                            head = acc;
-                        hs = true;
-                        ++seg;
-                        acc = vv_zero<VT, V>();
-                    }
-#pragma unroll
-                    for (int q = 0; q < V; ++q)
-                        acc.a[q] = fma(v[r0 + r], x[r].a[q], acc.a[q]);
-                }
-            };
-            if constexpr (sizeof(VT) == 4 && V == 1) {
-                // f32, one value per lane: the next column's gathers are in flight while this one accumulates
-                W xa[RB], xb[RB];
-                gather(c0, 0, xa);
-#pragma unroll 1
-                for (uint32_t cc = 0; cc < (uint32_t)LG; cc += 2) {
-                    gather(c0 + cc + 1, 0, xb);
-                    walk(c0 + cc, 0, xa);
-                    if (cc + 2 < (uint32_t)LG)
-                        gather(c0 + cc + 2, 0, xa);
-                    walk(c0 + cc + 1, 0, xb);
-                }
-            } else {
-#pragma unroll 1
-                for (uint32_t cc = 0; cc < (uint32_t)LG; ++cc) {
-#pragma unroll
-                    for (int r0 = 0; r0 < kSigma; r0 += RB) {
-                        W xv[RB];
-                        gather(c0 + cc, r0, xv);
-                        walk(c0 + cc, r0, xv);
-                    }
-                }
-            }
-            if (!hs)
-                head = acc;
-
-            // ---- join the groups in order: rows spanning groups, the tile's head and open segments ----
-            W open_v = vv_zero<VT, V>(), H = vv_zero<VT, V>();
-            uint32_t open_seg = 0;
-            bool closed0 = false;
-#pragma unroll
-            for (int gg = 0; gg < NG; ++gg) {
-                const int src = gg * LG + (int)j;
-                const uint32_t ghs = __shfl_sync(kFull, hs ? 1u : 0u, src);
-                const W ghd = vv_shfl<VT, V>(head, src);
-                const W gtl = vv_shfl<VT, V>(acc, src);
-                const uint32_t gseg = __shfl_sync(kFull, seg, src);
-                vv_add<VT, V>(open_v, ghd);
-                if (ghs) {
-                    if (open_seg == 0) {
-                        H = open_v;
-                        closed0 = true;
-                    } else {
-                        put_row(g == (unsigned)gg, row_of(open_seg), open_v);
-                    }
-                    open_v = gtl;
-                    open_seg = gseg;
-                }
-            }
-            if (!closed0)
-                H = open_v;
-            const uint32_t K = open_seg + 1;
-            const W Lt = open_v;
-            const uint32_t row_last = (K == 1) ? row_start : row_of(open_seg);
-
-            // ---- in-order carry chain over the warp's tiles (per right-hand side, same in every group) ----
-            if (K == 1) {
-                if (capped) {
-                    if (open)
-                        put_row(g == 0, carry_row, carry);
-                    open = true;
-                    carry = H;
-                    carry_row = row_start;
-                } else if (open) {
-                    vv_add<VT, V>(carry, H);
-                } else {
-                    vv_add<VT, V>(cal, H);
-                    cal_row = row_start;
-                    cal_valid = true;
-                }
-            } else {
-                if (capped) {
-                    if (open)
-                        put_row(g == 0, carry_row, carry);
-                    put_row(g == 0, row_start, H);
-                } else if (open) {
-                    put_row(g == 0, row_start, vv_sum<VT, V>(carry, H));
-                } else {
-                    vv_add<VT, V>(cal, H);
-                    cal_row = row_start;
-                    cal_valid = true;
-                }
-                open = true;
-                carry = Lt;
-                carry_row = row_last;
-            }
-            if constexpr (DOT) {
-#pragma unroll
-                for (int q = 0; q < V; ++q) {
-                    dot_acc[q] += (double)tdot.a[q];
-                    tdot.a[q] = VT(0);
-                }
+            // ---- rows that cross chunks: publish this chunk's fragment, finish the rows that end here ----
+            bool cont_after;
+            if (ce < p.T)
+                cont_after = ((__ldg(&p.desc[ce * 32]) >> (G::F.yb + G::F.sb)) & 1u) == 0;
+            else
+                cont_after = p.tail_start < p.rows && (uint64_t)p.row_ptr[p.tail_start] != p.T * kTS;
+            const bool through = cal_valid && !open;
+            uint32_t kind = kFragNone;
+            if (open && cont_after)
+                kind = kFragCarry;
+            else if (through && cont_after)
+                kind = kFragThrough;
+            if (kind != kFragNone && g == 0) {
+                const W& fv = kind == kFragCarry ? carry : cal;
+    #pragma unroll
+                for (int q = 0; q < V; ++q)
+                    p.frag_val[(uint64_t)c * 32 + j * V + q] = (double)fv.a[q];
+                if (j == 0)
+                    p.frag_row[c] = kind == kFragCarry ? carry_row : cal_row;
+                __threadfence();
             }
             __syncwarp();
-            if (lane == 0 && t + STAGES < t_end) {
-                fence_proxy_async_smem();
-                issue(s, t + STAGES);
-            }
-        }
-        if (failed) {
-            for (uint64_t t2 = t_begin + i; t2 < t_end && t2 < t_begin + i + STAGES; ++t2) {
-                const uint64_t i2 = t2 - t_begin;
-                (void)mbar_wait_bounded(&bars[i2 % STAGES], (uint32_t)((i2 / STAGES) & 1), p.status);
-            }
-        }
-
-        // ---- rows that cross runs: publish this run's fragment, finish the rows that end here ----
-        bool cont_after;
-        if (t_end < p.T)
-            cont_after = ((__ldg(&p.desc[t_end * 32]) >> (G::F.yb + G::F.sb)) & 1u) == 0;
-        else
-            cont_after = p.tail_start < p.rows && (uint64_t)p.row_ptr[p.tail_start] != p.T * kTS;
-        const bool through = cal_valid && !open;
-        uint32_t kind = kFragNone;
-        if (open && cont_after)
-            kind = kFragCarry;
-        else if (through && cont_after)
-            kind = kFragThrough;
-        if (kind != kFragNone && g == 0) {
-            const W& fv = kind == kFragCarry ? carry : cal;
-#pragma unroll
-            for (int q = 0; q < V; ++q)
-                p.frag_val[(uint64_t)run * 32 + j * V + q] = (double)fv.a[q];
-            if (j == 0)
-                p.frag_row[run] = kind == kFragCarry ? carry_row : cal_row;
-            __threadfence();
-        }
-        __syncwarp();
-        if (lane == 0)
-            st_release_u32(&p.flag[run], (epoch << 2) | kind);
-        if (open && !cont_after)
-            put_row(g == 0, carry_row, carry);
-        if (cal_valid && (!through || !cont_after)) {
-            // look back for the run where cal_row began, then add the fragments in run order
-            uint32_t first = run;
-            if (lane == 0) {
-                while (first > 0) {
-                    --first;
-                    const uint32_t kd = wait_run(&p.flag[first], epoch, p.status);
-                    if (__ldcg(&p.frag_row[first]) != cal_row || kd == kFragNone) {
-                        record_status(p.status, kStatusBadIndex);
-                        first = run;
-                        break;
+            if (lane == 0)
+                st_release_u32(&p.flag[c], (epoch << 2) | kind);
+            if (open && !cont_after)
+                put_row(g == 0, carry_row, carry);
+            if (cal_valid && (!through || !cont_after)) {
+                // look back for the chunk where cal_row began, then add the fragments in chunk order
+                uint32_t first = (uint32_t)c;
+                if (lane == 0) {
+                    while (first > 0) {
+                        --first;
+                        const uint32_t kd = wait_run(&p.flag[first], epoch, p.status);
+                        if (__ldcg(&p.frag_row[first]) != cal_row || kd == kFragNone) {
+                            record_status(p.status, kStatusBadIndex);
+                            first = (uint32_t)c;
+                            break;
+                        }
+                        if (kd == kFragCarry)
+                            break;
                     }
-                    if (kd == kFragCarry)
-                        break;
                 }
-            }
-            first = __shfl_sync(kFull, first, 0);
-            W v = vv_zero<VT, V>();
-            if (first < run && g == 0) {
-#pragma unroll
-                for (int q = 0; q < V; ++q) {
-                    VT a = (VT)__ldcg(&p.frag_val[(uint64_t)first * 32 + j * V + q]);
-                    for (uint32_t k2 = first + 1; k2 < run; ++k2)
-                        a += (VT)__ldcg(&p.frag_val[(uint64_t)k2 * 32 + j * V + q]);
-                    v.a[q] = a;
+                first = __shfl_sync(kFull, first, 0);
+                W v = vv_zero<VT, V>();
+                if (first < (uint32_t)c && g == 0) {
+    #pragma unroll
+                    for (int q = 0; q < V; ++q) {
+                        VT a = (VT)__ldcg(&p.frag_val[(uint64_t)first * 32 + j * V + q]);
+                        for (uint32_t k2 = first + 1; k2 < (uint32_t)c; ++k2)
+                            a += (VT)__ldcg(&p.frag_val[(uint64_t)k2 * 32 + j * V + q]);
+                        v.a[q] = a;
+                    }
                 }
+                put_row(g == 0, cal_row, vv_sum<VT, V>(v, cal));
             }
-            put_row(g == 0, cal_row, vv_sum<VT, V>(v, cal));
         }
     }
     if constexpr (DOT) {
@@ -522,7 +548,7 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
             double d = 0.0;
             for (int w = 0; w < WPC; ++w)
                 d += s_dot[w][threadIdx.x];
-            p.cta_part[(uint64_t)cta * 32 + threadIdx.x] = d;
+            p.cta_part[(uint64_t)blockIdx.x * 32 + threadIdx.x] = d;
         }
     }
     __syncthreads();
@@ -537,7 +563,7 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
 
     double fix_dot = 0.0;
     const uint64_t first_tail = p.T * kTS;
-    const uint32_t nruns = p.T ? (uint32_t)((p.T + p.tpw - 1) / p.tpw) : 0u;
+    const uint32_t nruns = p.nchunks;
     const bool lane_on = lane < p.k;
     for (uint64_t r = (uint64_t)p.tail_start + warp; r < p.rows; r += WPC) {
         const uint64_t s0 = (r == p.tail_start) ? first_tail : (uint64_t)p.row_ptr[r];
@@ -619,9 +645,15 @@ cudaError_t mm_attr() {
 template <typename VT, int KP, int V, int WPC, int STAGES, bool DOT>
 int mm_launch(const dimgpu_csr5* m, const VT* vals, const spmm_args& a, const spmm_scratch& sc, cudaStream_t st) {
     const spmv_plan pl = make_spmv_plan(m->tile_count, device_sm_count(m->device), WPC);
-    if (pl.nwarps > sc.nslots)
-        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "SpMM scratch holds %u warp slots, launch needs %u", sc.nslots,
-                    pl.nwarps);
+    // about kSpmmRounds chunks per warp (as many as the scratch holds), at least STAGES tiles each
+    const uint64_t T = m->tile_count;
+    const uint64_t target =
+        std::max<uint64_t>(1, std::min<uint64_t>(sc.nslots, (uint64_t)kSpmmRounds * pl.nwarps));
+    const uint64_t chunk = std::max<uint64_t>(STAGES, (T + target - 1) / target);
+    const uint64_t nchunks = T ? (T + chunk - 1) / chunk : 0;
+    if (nchunks > sc.nslots)
+        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "SpMM scratch holds %u chunk slots, launch needs %llu", sc.nslots,
+                    (unsigned long long)nchunks);
     spmm_params<VT> p;
     p.vals = vals;
     p.col = m->col;
@@ -638,8 +670,8 @@ int mm_launch(const dimgpu_csr5* m, const VT* vals, const spmm_args& a, const sp
     p.T = m->tile_count;
     p.rows = m->rows;
     p.tail_start = m->tail_start;
-    p.tpw = pl.tiles_per_warp;
-    p.nwarps = pl.nwarps;
+    p.chunk = chunk;
+    p.nchunks = (uint32_t)nchunks;
     p.empty_rows = m->empty_rows;
     p.n_empty = m->n_empty;
     p.frag_val = sc.cal_val;
@@ -654,8 +686,18 @@ int mm_launch(const dimgpu_csr5* m, const VT* vals, const spmm_args& a, const sp
     p.mask = a.mask;
     p.mask_sel = a.mask_sel;
     p.halt = a.halt;
-    k_spmm<VT, KP, V, WPC, STAGES, DOT><<<pl.grid, WPC * 32, mm_smem<VT, WPC, STAGES>(), st>>>(p);
-    DG_CUDA(cudaGetLastError());
+    // cooperative: every CTA resident (one per SM), so chunks can wait on each other's fragments
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(pl.grid);
+    cfg.blockDim = dim3(WPC * 32);
+    cfg.dynamicSmemBytes = mm_smem<VT, WPC, STAGES>();
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    DG_CUDA(cudaLaunchKernelEx(&cfg, k_spmm<VT, KP, V, WPC, STAGES, DOT>, p));
     return DIMGPU_OK;
 }
 
@@ -746,7 +788,7 @@ uint32_t spmm_max_slots(const dimgpu_csr5* m) {
     uint32_t n = 1;
     for (int wpc : {8, 16})
         n = std::max<uint32_t>(n, make_spmv_plan(m->tile_count, sms, wpc).nwarps);
-    return n;
+    return n * kSpmmRounds;
 }
 
 int spmm_scratch_init(spmm_scratch* s, const dimgpu_csr5* m) {
