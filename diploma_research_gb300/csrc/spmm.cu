@@ -214,6 +214,12 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const unsigned g = lane / LG, j = lane % LG;
     const bool active = j * V < p.k;  // the host sends V > 1 only when k is a multiple of V
+    // Lane bases of X and Y: inactive lanes gather from the last active lane's columns (valid addresses,
+    // values never stored), so the gathers need no select; row offsets are widening 32 x 32-bit products.
+    const uint32_t jj = min(j, (uint32_t)(p.k / V) - 1u);
+    const VT* __restrict__ Xl = p.X + jj * V;
+    VT* __restrict__ Yl = p.Y + jj * V;
+    const uint32_t ldx = (uint32_t)p.ldx, ldy = (uint32_t)p.ldy;
     if (threadIdx.x == 0)
         s_epoch = *reinterpret_cast<volatile const uint32_t*>(&p.words[3]) + 1u;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem) + warp * STAGES;
@@ -245,9 +251,9 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
     // k-wide row write by the lanes of one group (`mine`), with its share of the dot
     auto put_row = [&](bool mine, uint32_t row, const W& val) {
         if (mine && active) {
-            st_vec<VT, V>(p.Y + (uint64_t)row * p.ldy + j * V, val);
+            st_vec<VT, V>(Yl + (uint64_t)row * ldy, val);
             if constexpr (DOT) {
-                const W xr = ldg_vec<VT, V>(p.X + (uint64_t)row * p.ldx + j * V, pol_keep);
+                const W xr = ldg_vec<VT, V>(Xl + (uint64_t)row * ldx, pol_keep);
 #pragma unroll
                 for (int i = 0; i < V; ++i)
                     tdot.a[i] = fma(val.a[i], xr.a[i], tdot.a[i]);
@@ -330,8 +336,7 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
                     stage_cols(st + G::VBYTES, c, ci);
     #pragma unroll
                     for (int r = 0; r < RB; ++r)
-                        x[r] = active ? ldg_vec<VT, V>(p.X + (uint64_t)ci[r0 + r] * p.ldx + j * V, pol_keep)
-                                      : vv_zero<VT, V>();
+                        x[r] = ldg_vec<VT, V>(Xl + (uint64_t)ci[r0 + r] * ldx, pol_keep);
                 };
                 // rows [r0, r0 + RB) of tile column c, in CSR order, with their gathered x
                 auto walk = [&](uint32_t c, int r0, const W (&x)[RB]) {
@@ -823,6 +828,8 @@ int launch_spmm(const dimgpu_csr5* m, bool f32, const spmm_args& a, const spmm_s
         return fail(DIMGPU_ERR_INVALID_ARGUMENT, "one SpMM pass takes 1..32 right-hand sides (got %u)", a.k);
     if (a.ldx < a.k || a.ldy < a.k)
         return fail(DIMGPU_ERR_INVALID_ARGUMENT, "leading dimensions must be >= k");
+    if (a.ldx > 0xffffffffull || a.ldy > 0xffffffffull)
+        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "leading dimensions must be < 2^32");
     const bool dot = a.dot_out || a.alpha_out;
     if (f32) {
         DG_CHECK(ensure_vals32(m, st));
