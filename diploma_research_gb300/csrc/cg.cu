@@ -112,19 +112,27 @@ __device__ __forceinline__ void set_ru(const vec_ctx& c, bool go) {
         cudaGraphSetConditional(c.ru, go ? 1u : 0u);
 }
 
-// Calls f(i) for every vector index i in [0, nv): each thread takes U elements one grid stride apart
-// per round (guarded), so that their independent 16-byte loads are in flight together.  The grid is two
-// resident blocks per SM (every kernel here is register-bounded to allow that), so one wave covers it.
-template <int U = kUnroll, typename F>
-__device__ __forceinline__ void vloop(uint64_t nv, F f) {
+// Visits every vector index i in [0, nv): each thread takes U indices one grid stride apart per round
+// and calls load(i, u) for all U of them before op(i, u) for any, so that the round's independent
+// 16-byte loads are in flight together (op's stores may alias the next loads as far as the compiler
+// knows, so interleaving the two would cost one memory round trip per element).  Indices left after the
+// last full round go one at a time, in the same order.  The grid is two resident blocks per SM (every
+// kernel here is register-bounded to allow that), so one wave covers it.
+template <int U = kUnroll, typename Ld, typename Op>
+__device__ __forceinline__ void vloop(uint64_t nv, Ld load, Op op) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; base < nv; base += U * stride) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    for (; i + (U - 1) * stride < nv; i += U * stride) {
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const uint64_t i = base + u * stride;
-            if (i < nv)
-                f(i);
-        }
+        for (int u = 0; u < U; ++u)
+            load(i + u * stride, u);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            op(i + u * stride, u);
+    }
+    for (; i < nv; i += stride) {
+        load(i, 0);
+        op(i, 0);
     }
 }
 
@@ -145,14 +153,22 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_init64(const double* b, cons
                                                         uint64_t n, vec_ctx c) {
     const uint64_t pol = policy_evict_last();
     double rr = 0, bb = 0;
-    vloop(n / 2, [&](uint64_t i) {
-        const double2 bi = ld2_keep(b + 2 * i, pol), ai = ld2_keep(Ax + 2 * i, pol);
-        const double2 ri = make_double2(bi.x - ai.x, bi.y - ai.y);
-        st2_stream(r + 2 * i, ri, pol);
-        st2_stream(s + 2 * i, ri, pol);
-        rr = fma(ri.x, ri.x, fma(ri.y, ri.y, rr));
-        bb = fma(bi.x, bi.x, fma(bi.y, bi.y, bb));
-    });
+    constexpr int U = 1;  // runs once per solve; one element per round keeps it free of spills
+    double2 bv[U], av[U];
+    vloop<U>(
+        n / 2,
+        [&](uint64_t i, int u) {
+            bv[u] = ld2_keep(b + 2 * i, pol);
+            av[u] = ld2_keep(Ax + 2 * i, pol);
+        },
+        [&](uint64_t i, int u) {
+            const double2 bi = bv[u], ai = av[u];
+            const double2 ri = make_double2(bi.x - ai.x, bi.y - ai.y);
+            st2_stream(r + 2 * i, ri, pol);
+            st2_stream(s + 2 * i, ri, pol);
+            rr = fma(ri.x, ri.x, fma(ri.y, ri.y, rr));
+            bb = fma(bi.x, bi.x, fma(bi.y, bi.y, bb));
+        });
     vtail(n, 2, [&](uint64_t i) {
         const double ri = b[i] - Ax[i];
         r[i] = ri;
@@ -189,14 +205,21 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_update_r64(const double* As,
     }
     const uint64_t pol = policy_evict_last();
     double rr = 0;
-    vloop(n / 2, [&](uint64_t i) {
-        const double2 a = ld2_keep(As + 2 * i, pol);
-        double2 q = ld2_keep(r + 2 * i, pol);
-        q.x = fma(-alpha, a.x, q.x);
-        q.y = fma(-alpha, a.y, q.y);
-        st2_stream(r + 2 * i, q, pol);
-        rr = fma(q.x, q.x, fma(q.y, q.y, rr));
-    });
+    double2 av[kUnroll], qv[kUnroll];
+    vloop(
+        n / 2,
+        [&](uint64_t i, int u) {
+            av[u] = ld2_keep(As + 2 * i, pol);
+            qv[u] = ld2_keep(r + 2 * i, pol);
+        },
+        [&](uint64_t i, int u) {
+            const double2 a = av[u];
+            double2 q = qv[u];
+            q.x = fma(-alpha, a.x, q.x);
+            q.y = fma(-alpha, a.y, q.y);
+            st2_stream(r + 2 * i, q, pol);
+            rr = fma(q.x, q.x, fma(q.y, q.y, rr));
+        });
     vtail(n, 2, [&](uint64_t i) {
         const double ri = fma(-alpha, As[i], r[i]);
         r[i] = ri;
@@ -229,22 +252,37 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_update_xs64(double* x, doubl
         return;
     const uint64_t pol = policy_evict_last();
     const bool more = !stop;
+    constexpr int U = 3;  // three 16-byte loads per element: 36 registers of loaded data per round
+    double2 sv[U], xv[U], rv[U];
     if (more) {
-        vloop<2>(n / 2, [&](uint64_t i) {
-            const double2 si = ld2_keep(s + 2 * i, pol), xi = ld2_keep(x + 2 * i, pol), ri = ld2_keep(r + 2 * i, pol);
-            st2_stream(x + 2 * i, make_double2(fma(alpha, si.x, xi.x), fma(alpha, si.y, xi.y)), pol);
-            st2_stream(s + 2 * i, make_double2(fma(beta, si.x, ri.x), fma(beta, si.y, ri.y)), pol);
-        });
+        vloop<U>(
+            n / 2,
+            [&](uint64_t i, int u) {
+                sv[u] = ld2_keep(s + 2 * i, pol);
+                xv[u] = ld2_keep(x + 2 * i, pol);
+                rv[u] = ld2_keep(r + 2 * i, pol);
+            },
+            [&](uint64_t i, int u) {
+                const double2 si = sv[u], xi = xv[u], ri = rv[u];
+                st2_stream(x + 2 * i, make_double2(fma(alpha, si.x, xi.x), fma(alpha, si.y, xi.y)), pol);
+                st2_stream(s + 2 * i, make_double2(fma(beta, si.x, ri.x), fma(beta, si.y, ri.y)), pol);
+            });
         vtail(n, 2, [&](uint64_t i) {
             const double si = s[i];
             x[i] = fma(alpha, si, x[i]);
             s[i] = fma(beta, si, r[i]);
         });
     } else {
-        vloop<2>(n / 2, [&](uint64_t i) {
-            const double2 si = ld2_keep(s + 2 * i, pol), xi = ld2_keep(x + 2 * i, pol);
-            st2_stream(x + 2 * i, make_double2(fma(alpha, si.x, xi.x), fma(alpha, si.y, xi.y)), pol);
-        });
+        vloop<U>(
+            n / 2,
+            [&](uint64_t i, int u) {
+                sv[u] = ld2_keep(s + 2 * i, pol);
+                xv[u] = ld2_keep(x + 2 * i, pol);
+            },
+            [&](uint64_t i, int u) {
+                const double2 si = sv[u], xi = xv[u];
+                st2_stream(x + 2 * i, make_double2(fma(alpha, si.x, xi.x), fma(alpha, si.y, xi.y)), pol);
+            });
         vtail(n, 2, [&](uint64_t i) { x[i] = fma(alpha, s[i], x[i]); });
     }
 }
@@ -260,17 +298,26 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_init_mixed(const double* b, 
                                                             float* y32, uint64_t n, vec_ctx c) {
     const uint64_t pol = policy_evict_last();
     double rr = 0, bb = 0;
-    vloop(n / 4, [&](uint64_t i) {
-        const double2 b0 = ld2_keep(b + 4 * i, pol), b1 = ld2_keep(b + 4 * i + 2, pol);
-        const double2 a0 = ld2_keep(Ax + 4 * i, pol), a1 = ld2_keep(Ax + 4 * i + 2, pol);
-        const double r0 = b0.x - a0.x, r1 = b0.y - a0.y, r2 = b1.x - a1.x, r3 = b1.y - a1.y;
-        const float4 rf = make_float4((float)r0, (float)r1, (float)r2, (float)r3);
-        st4_stream(r32 + 4 * i, rf, pol);
-        st4_stream(s32 + 4 * i, rf, pol);
-        st4_stream(y32 + 4 * i, make_float4(0.f, 0.f, 0.f, 0.f), pol);
-        rr = fma(r0, r0, fma(r1, r1, fma(r2, r2, fma(r3, r3, rr))));
-        bb = fma(b0.x, b0.x, fma(b0.y, b0.y, fma(b1.x, b1.x, fma(b1.y, b1.y, bb))));
-    });
+    constexpr int U = 1;  // four 16-byte loads per element; runs once per solve
+    double2 b0v[U], b1v[U], a0v[U], a1v[U];
+    vloop<U>(
+        n / 4,
+        [&](uint64_t i, int u) {
+            b0v[u] = ld2_keep(b + 4 * i, pol);
+            b1v[u] = ld2_keep(b + 4 * i + 2, pol);
+            a0v[u] = ld2_keep(Ax + 4 * i, pol);
+            a1v[u] = ld2_keep(Ax + 4 * i + 2, pol);
+        },
+        [&](uint64_t i, int u) {
+            const double2 b0 = b0v[u], b1 = b1v[u], a0 = a0v[u], a1 = a1v[u];
+            const double r0 = b0.x - a0.x, r1 = b0.y - a0.y, r2 = b1.x - a1.x, r3 = b1.y - a1.y;
+            const float4 rf = make_float4((float)r0, (float)r1, (float)r2, (float)r3);
+            st4_stream(r32 + 4 * i, rf, pol);
+            st4_stream(s32 + 4 * i, rf, pol);
+            st4_stream(y32 + 4 * i, make_float4(0.f, 0.f, 0.f, 0.f), pol);
+            rr = fma(r0, r0, fma(r1, r1, fma(r2, r2, fma(r3, r3, rr))));
+            bb = fma(b0.x, b0.x, fma(b0.y, b0.y, fma(b1.x, b1.x, fma(b1.y, b1.y, bb))));
+        });
     vtail(n, 4, [&](uint64_t i) {
         const double ri = b[i] - Ax[i];
         r32[i] = (float)ri;
@@ -314,15 +361,26 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_update_r_mixed(const float* 
     }
     const uint64_t pol = policy_evict_last();
     double rr = 0;
-    vloop(n / 4, [&](uint64_t i) {
-        const float4 a = ld4_keep(As + 4 * i, pol), si = ld4_keep(s + 4 * i, pol);
-        float4 q = ld4_keep(r + 4 * i, pol), yi = ld4_keep(y + 4 * i, pol);
-        q = make_float4(fmaf(-af, a.x, q.x), fmaf(-af, a.y, q.y), fmaf(-af, a.z, q.z), fmaf(-af, a.w, q.w));
-        yi = make_float4(fmaf(af, si.x, yi.x), fmaf(af, si.y, yi.y), fmaf(af, si.z, yi.z), fmaf(af, si.w, yi.w));
-        st4_stream(r + 4 * i, q, pol);
-        st4_stream(y + 4 * i, yi, pol);
-        rr += (double)sq4(q);
-    });
+    constexpr int U = 2;  // four 16-byte loads per element
+    float4 av[U], sv[U], qv[U], yv[U];
+    vloop<U>(
+        n / 4,
+        [&](uint64_t i, int u) {
+            av[u] = ld4_keep(As + 4 * i, pol);
+            sv[u] = ld4_keep(s + 4 * i, pol);
+            qv[u] = ld4_keep(r + 4 * i, pol);
+            yv[u] = ld4_keep(y + 4 * i, pol);
+        },
+        [&](uint64_t i, int u) {
+            const float4 a = av[u], si = sv[u];
+            float4 q = qv[u], yi = yv[u];
+            q = make_float4(fmaf(-af, a.x, q.x), fmaf(-af, a.y, q.y), fmaf(-af, a.z, q.z), fmaf(-af, a.w, q.w));
+            yi = make_float4(fmaf(af, si.x, yi.x), fmaf(af, si.y, yi.y), fmaf(af, si.z, yi.z),
+                             fmaf(af, si.w, yi.w));
+            st4_stream(r + 4 * i, q, pol);
+            st4_stream(y + 4 * i, yi, pol);
+            rr += (double)sq4(q);
+        });
     vtail(n, 4, [&](uint64_t i) {
         const float q = fmaf(-af, As[i], r[i]);
         r[i] = q;
@@ -351,13 +409,23 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_flush_mixed(double* x, float
     if (guarded && *reinterpret_cast<const volatile uint32_t*>(&st->no_ru))
         return;
     const uint64_t pol = policy_evict_last();
-    vloop(n / 4, [&](uint64_t i) {
-        const float4 yi = ld4_keep(y + 4 * i, pol);
-        const double2 x0 = ld2_keep(x + 4 * i, pol), x1 = ld2_keep(x + 4 * i + 2, pol);
-        st2_stream(x + 4 * i, make_double2(x0.x + (double)yi.x, x0.y + (double)yi.y), pol);
-        st2_stream(x + 4 * i + 2, make_double2(x1.x + (double)yi.z, x1.y + (double)yi.w), pol);
-        st4_stream(y + 4 * i, make_float4(0.f, 0.f, 0.f, 0.f), pol);
-    });
+    constexpr int U = 2;  // three 16-byte loads per element
+    float4 yv[U];
+    double2 x0v[U], x1v[U];
+    vloop<U>(
+        n / 4,
+        [&](uint64_t i, int u) {
+            yv[u] = ld4_keep(y + 4 * i, pol);
+            x0v[u] = ld2_keep(x + 4 * i, pol);
+            x1v[u] = ld2_keep(x + 4 * i + 2, pol);
+        },
+        [&](uint64_t i, int u) {
+            const float4 yi = yv[u];
+            const double2 x0 = x0v[u], x1 = x1v[u];
+            st2_stream(x + 4 * i, make_double2(x0.x + (double)yi.x, x0.y + (double)yi.y), pol);
+            st2_stream(x + 4 * i + 2, make_double2(x1.x + (double)yi.z, x1.y + (double)yi.w), pol);
+            st4_stream(y + 4 * i, make_float4(0.f, 0.f, 0.f, 0.f), pol);
+        });
     vtail(n, 4, [&](uint64_t i) {
         x[i] += (double)y[i];
         y[i] = 0.f;
@@ -372,13 +440,22 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_ru_r_mixed(const double* b, 
         return;
     const uint64_t pol = policy_evict_last();
     double rr = 0;
-    vloop(n / 4, [&](uint64_t i) {
-        const double2 b0 = ld2_keep(b + 4 * i, pol), b1 = ld2_keep(b + 4 * i + 2, pol);
-        const double2 a0 = ld2_keep(Ax + 4 * i, pol), a1 = ld2_keep(Ax + 4 * i + 2, pol);
-        const double r0 = b0.x - a0.x, r1 = b0.y - a0.y, r2 = b1.x - a1.x, r3 = b1.y - a1.y;
-        st4_stream(r32 + 4 * i, make_float4((float)r0, (float)r1, (float)r2, (float)r3), pol);
-        rr = fma(r0, r0, fma(r1, r1, fma(r2, r2, fma(r3, r3, rr))));
-    });
+    constexpr int U = 2;  // four 16-byte loads per element
+    double2 b0v[U], b1v[U], a0v[U], a1v[U];
+    vloop<U>(
+        n / 4,
+        [&](uint64_t i, int u) {
+            b0v[u] = ld2_keep(b + 4 * i, pol);
+            b1v[u] = ld2_keep(b + 4 * i + 2, pol);
+            a0v[u] = ld2_keep(Ax + 4 * i, pol);
+            a1v[u] = ld2_keep(Ax + 4 * i + 2, pol);
+        },
+        [&](uint64_t i, int u) {
+            const double2 b0 = b0v[u], b1 = b1v[u], a0 = a0v[u], a1 = a1v[u];
+            const double r0 = b0.x - a0.x, r1 = b0.y - a0.y, r2 = b1.x - a1.x, r3 = b1.y - a1.y;
+            st4_stream(r32 + 4 * i, make_float4((float)r0, (float)r1, (float)r2, (float)r3), pol);
+            rr = fma(r0, r0, fma(r1, r1, fma(r2, r2, fma(r3, r3, rr))));
+        });
     vtail(n, 4, [&](uint64_t i) {
         const double ri = b[i] - Ax[i];
         r32[i] = (float)ri;
@@ -410,13 +487,20 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_update_s_mixed(float* s, con
     if (stop)
         return;
     const uint64_t pol = policy_evict_last();
-    vloop(n / 4, [&](uint64_t i) {
-        const float4 si = ld4_keep(s + 4 * i, pol), ri = ld4_keep(r + 4 * i, pol);
-        st4_stream(s + 4 * i,
-                 make_float4(fmaf(beta, si.x, ri.x), fmaf(beta, si.y, ri.y), fmaf(beta, si.z, ri.z),
-                             fmaf(beta, si.w, ri.w)),
-                 pol);
-    });
+    float4 sv[kUnroll], rv[kUnroll];
+    vloop(
+        n / 4,
+        [&](uint64_t i, int u) {
+            sv[u] = ld4_keep(s + 4 * i, pol);
+            rv[u] = ld4_keep(r + 4 * i, pol);
+        },
+        [&](uint64_t i, int u) {
+            const float4 si = sv[u], ri = rv[u];
+            st4_stream(s + 4 * i,
+                       make_float4(fmaf(beta, si.x, ri.x), fmaf(beta, si.y, ri.y), fmaf(beta, si.z, ri.z),
+                                   fmaf(beta, si.w, ri.w)),
+                       pol);
+        });
     vtail(n, 4, [&](uint64_t i) { s[i] = fmaf(beta, s[i], r[i]); });
 }
 
