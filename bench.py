@@ -406,6 +406,41 @@ def run_spmv_only(args):
     return 0
 
 
+def run_spmm_only(args):
+    """A short SpMM-only run (few launches) for profiler captures: k right-hand sides U[-1, 1] (seed 6),
+    the launch-shape autotuning call, 5 warm-up launches, then `steps` timed launches."""
+    import numpy as np
+    import torch
+
+    from diploma_research_gb300 import build as B
+
+    B.build()
+    from diploma_research_gb300.csr5 import csr5, spmm, spmm_shape
+
+    m, _, _ = _workload()
+    n, nnz, k = m.dimensions.rows, m.nnz, int(args.spmm_only)
+    A = csr5.from_csr(m)
+    dt = torch.float32 if args.f32 else torch.float64
+    X = torch.tensor(np.random.default_rng(6).uniform(-1, 1, (n, k)), device="cuda", dtype=dt)
+    Y = torch.empty((n, k), device="cuda", dtype=dt)
+    for _ in range(5):
+        spmm(A, X, Y)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        spmm(A, X, Y)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    s = ev0.elapsed_time(ev1) * 1e-3 / args.steps
+    w = 4 if args.f32 else 8
+    nbytes = (w + 4) * nnz + 2 * w * n * k
+    print(json.dumps({"spmm_seconds": s, "gbps": nbytes / s / 1e9, "k": k, "nnz": nnz, "n": n, "f32": bool(args.f32),
+                      "shape": spmm_shape(A, k, bool(args.f32))}))
+    return 0
+
+
 def run_batch(args):
     """Multi-RHS workload: 3-D 7-point Laplacian 192^3 (n = 7,077,888), k right-hand sides b_j = A x*_j
     (x* ~ U[-1,1], seed 3), block CG to 1e-10 per column in FP64 and mixed precision, against k separate
@@ -556,7 +591,9 @@ def main():
     ap.add_argument("--impl", default="dimgpu", choices=["dimgpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--spmv-only", action="store_true", help="few SpMV launches only (for profiler captures)")
-    ap.add_argument("--f32", action="store_true", help="with --spmv-only: the f32 product")
+    ap.add_argument("--spmm-only", type=int, default=0, metavar="K",
+                    help="few SpMM launches with K right-hand sides only (for profiler captures)")
+    ap.add_argument("--f32", action="store_true", help="with --spmv-only / --spmm-only: the f32 product")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven CG loop instead of the CUDA graph (profilers list every kernel)")
     ap.add_argument("--batch", default=None, help="comma-separated k: the multi-RHS block-CG workload")
@@ -573,6 +610,8 @@ def main():
         return run_batch(args)
     if args.spmv_only:
         return run_spmv_only(args)
+    if args.spmm_only:
+        return run_spmm_only(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
