@@ -24,6 +24,8 @@ where this was built, so interoperability with them is by construction, not by t
 """
 from __future__ import annotations
 
+import mmap
+import os
 import struct
 import zlib
 from dataclasses import dataclass, field
@@ -287,8 +289,9 @@ def _parse_space(b: bytes, p: int) -> tuple:
 
 class _File:
     def __init__(self, path):
+        # mapped, not read: a slab read touches only the pages of its bytes
         with open(path, "rb") as fh:
-            self.b = fh.read()
+            self.b = mmap.mmap(fh.fileno(), 0, access=mmap.ACCESS_READ) if os.path.getsize(path) else b""
         b = self.b
         if b[:8] != SIGNATURE:
             raise H5FormatError(f"{path} is not an HDF5 file")
@@ -301,6 +304,11 @@ class _File:
         self.base = struct.unpack_from("<Q", b, p)[0]
         p += 32
         self.root = struct.unpack_from("<Q", b, p + 8)[0] + self.base
+
+    def close(self):
+        if isinstance(self.b, mmap.mmap):
+            self.b.close()
+        self.b = b""
 
     def u64(self, p):
         return struct.unpack_from("<Q", self.b, p)[0]
@@ -356,7 +364,7 @@ class _File:
                     q = sn + 8 + 40 * e
                     name_off, oh = self.u64(q), self.u64(q + 8)
                     s = seg + name_off
-                    name = b[s:b.index(b"\0", s)].decode()
+                    name = b[s:b.find(b"\0", s)].decode()
                     members[name] = oh + self.base
 
         walk(tree)
@@ -383,6 +391,32 @@ class _File:
             val = np.frombuffer(d, typ.numpy(), n * max(1, typ.inner), p)
             out[name] = val[0] if n == 1 and not typ.inner else val.copy()
         return out
+
+    def read_slab(self, addr: int, start: int, count: int) -> np.ndarray:
+        """Elements [start, start + count) of a 1-D dataset: only those bytes for the contiguous layout
+        (the reference's read_slab, h5.h), a slice of the whole for the others."""
+        typ = shape = layout = None
+        for t, d in self.messages(addr):
+            if t == 0x0001:
+                shape = _parse_space(d, 0)
+            elif t == 0x0003:
+                typ, _ = _parse_type(d, 0)
+            elif t == 0x0008:
+                layout = d
+        if typ is None or shape is None or layout is None:
+            raise H5FormatError("not a dataset")
+        n = int(shape[0]) if shape else 1
+        if start < 0 or count < 0 or start + count > n:
+            raise ValueError(f"slab [{start}, {start + count}) of a dataset of {n}")
+        per = typ.size * max(1, typ.inner) if typ.inner else typ.size
+        if len(shape) == 1 and layout[0] == 3 and layout[1] == 1 and not typ.inner:
+            a, sz = struct.unpack_from("<QQ", layout, 2)
+            if a == UNDEF:
+                return np.zeros(count, typ.numpy())
+            lo = a + self.base + start * per
+            raw = bytes(self.b[lo:lo + count * per]).ljust(count * per, b"\0")
+            return np.frombuffer(raw, typ.numpy()).copy()
+        return self.read_dataset(addr)[start:start + count].copy()
 
     def read_dataset(self, addr: int) -> np.ndarray:
         typ = shape = layout = None
@@ -492,6 +526,16 @@ class H5Reader:
     def __init__(self, path):
         self.f = _File(path)
 
+    def close(self):
+        """Unmaps the file (a mapped file that another writer truncates must not be touched again)."""
+        self.f.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
     def _resolve(self, path: str) -> int:
         addr = self.f.root
         for part in _split(path):
@@ -510,6 +554,16 @@ class H5Reader:
     def dataset(self, path: str) -> np.ndarray:
         return self.f.read_dataset(self._resolve(path))
 
+    def dataset_slab(self, path: str, start: int, count: int) -> np.ndarray:
+        return self.f.read_slab(self._resolve(path), start, count)
+
+    def dataset_length(self, path: str) -> int:
+        for t, d in self.f.messages(self._resolve(path)):
+            if t == 0x0001:
+                shape = _parse_space(d, 0)
+                return int(shape[0]) if shape else 1
+        raise H5FormatError("not a dataset")
+
     def contains(self, path: str) -> bool:
         try:
             self._resolve(path)
@@ -526,7 +580,8 @@ class H5Writer:
         self.path = path
         self.root = _Group()
         if append and is_hdf5(path):
-            self._load(H5Reader(path), "/", self.root)
+            with H5Reader(path) as r:  # everything is copied out before the file is rewritten
+                self._load(r, "/", self.root)
 
     def _load(self, r: H5Reader, path: str, grp: _Group):
         grp.attrs.update(r.attributes(path))
@@ -588,11 +643,11 @@ def read_matlab_compatible(path, group: str = "A"):
     """include/dim/io/h5.h:72-90."""
     from ..mat import csr, dimensions_t
 
-    r = H5Reader(path)
-    jc = r.dataset(f"{group}/jc").astype(np.uint32)
-    cols = int(r.attributes(group)["MATLAB_sparse"])
-    return csr(dimensions_t(jc.size - 1, cols), r.dataset(f"{group}/data").astype(np.float64), jc,
-               r.dataset(f"{group}/ir").astype(np.uint32))
+    with H5Reader(path) as r:
+        jc = r.dataset(f"{group}/jc").astype(np.uint32)
+        cols = int(r.attributes(group)["MATLAB_sparse"])
+        return csr(dimensions_t(jc.size - 1, cols), r.dataset(f"{group}/data").astype(np.float64), jc,
+                   r.dataset(f"{group}/ir").astype(np.uint32))
 
 
 def store_csr5(path, group: str, arrays, cols: int, append: bool = False):
@@ -612,9 +667,13 @@ def store_csr5(path, group: str, arrays, cols: int, append: bool = False):
 
 def load_csr5_arrays(path, group: str = "A"):
     """libs/dim/io/h5.cpp:57-74: the stored arrays and the dimensions (rows = len(row_ptr) - 1)."""
+    with H5Reader(path) as r:
+        return _csr5_arrays(r, group)
+
+
+def _csr5_arrays(r, group: str):
     from types import SimpleNamespace
 
-    r = H5Reader(path)
     td = r.dataset(f"{group}/tile_desc")
     out = SimpleNamespace(
         vals=r.dataset(f"{group}/vals").astype(np.float64),
@@ -631,6 +690,42 @@ def load_csr5_arrays(path, group: str = "A"):
     return out
 
 
+def load_csr5_partial(path, group: str, part):
+    """Part `part` (a partial.partial_identifier_t) of a stored CSR5 matrix, reading only its slabs
+    (load_csr5_partial, h5.cpp:105-173): the stored tiles (sigma 16 x omega 4) are cut into runs of
+    ceil(T / parts), the last part also takes the CSR tail.  The chunk's tiles are put back into CSR order
+    (the inverse of csr5::transpose, csr5.h:463-493: a full tile whose rows differ was stored row-major
+    over its omega columns) and returned as a partial.partial_layout."""
+    with H5Reader(path) as r:
+        return _load_csr5_partial(r, group, part)
+
+
+def _load_csr5_partial(r, group: str, part):
+    from ..partial import REF_TILE, partial_layout
+
+    cols = int(r.attributes(group)["column_count"])
+    rows = r.dataset_length(f"{group}/row_ptr") - 1
+    nnz = r.dataset_length(f"{group}/vals")
+    tiles = r.dataset_length(f"{group}/tile_desc")
+    if tiles != nnz // REF_TILE:
+        raise H5FormatError(f"{tiles} stored tiles for {nnz} elements: not a sigma 16 x omega 4 CSR5 group")
+    start, count, e0, e1 = partial_layout.chunk_of(nnz, part)
+    tp = r.dataset_slab(f"{group}/tile_ptr", start, count + 1).astype(np.int64) & 0x7FFFFFFF
+    vals = r.dataset_slab(f"{group}/vals", e0, e1 - e0).astype(np.float64)
+    col = r.dataset_slab(f"{group}/col_idx", e0, e1 - e0).astype(np.uint32)
+    sigma, omega = 16, REF_TILE // 16
+    for i in range(count):
+        if tp[i] != tp[i + 1]:
+            blk = slice(i * REF_TILE, (i + 1) * REF_TILE)
+            vals[blk] = vals[blk].reshape(sigma, omega).T.reshape(-1)
+            col[blk] = col[blk].reshape(sigma, omega).T.reshape(-1)
+    # row offsets from the chunk's first row (tile_ptr[start]) to beyond its last row
+    r0 = int(tp[0])
+    r1 = rows if part.idx == part.total_count - 1 else min(rows, int(tp[-1]) + 1)
+    rp = r.dataset_slab(f"{group}/row_ptr", r0, r1 + 1 - r0)
+    return partial_layout.from_chunk(part, rows, cols, nnz, rp, r0, vals, col)
+
+
 def write_vector(path, dataset: str, y, overwrite: bool = False, append: bool = True):
     """The result dump of benchmarks/csr5/dim/main.cpp:35-43 (f64 dataset, refuses to overwrite unless asked)."""
     with H5Writer(path, append=append) as w:
@@ -642,4 +737,5 @@ def write_vector(path, dataset: str, y, overwrite: bool = False, append: bool = 
 
 
 def read_vector(path, dataset: str) -> np.ndarray:
-    return H5Reader(path).dataset(dataset).astype(np.float64)
+    with H5Reader(path) as r:
+        return r.dataset(dataset).astype(np.float64)
