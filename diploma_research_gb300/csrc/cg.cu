@@ -9,8 +9,8 @@
 //   A  SpMV As = A s fused with s.As and alpha = rr / s.As (spmv.cu's last-CTA epilogue)
 //   B  r -= alpha As and r.r; its last block decides convergence, beta and the loop condition
 //   C  x += alpha s and s = r + beta s in one pass (x is updated here, from the old s)
-// The whole solve is one CUDA graph: init kernels, then a conditional WHILE node whose body is the
-// iteration; kernel B sets the loop condition from the device, so the solve makes no host round trip.
+// The whole solve is one CUDA graph: init kernels, then a conditional WHILE node whose body is four
+// iterations; kernel B sets the loop condition from the device, so the solve makes no host round trip.
 //
 // Mixed precision runs the same recurrence on f32 values and f32 vectors s, As, r.  Products and short
 // partial sums are f32, every dot product is accumulated in f64, alpha and beta are f64, and the
@@ -666,8 +666,14 @@ int add_conditional(cudaGraph_t graph, const std::vector<cudaGraphNode_t>& deps,
     return DIMGPU_OK;
 }
 
-// Graph: init kernels -> WHILE(loop) { iteration }.  The mixed iteration is
-// A32 -> B32 -> IF(ru) { flush, f64 SpMV, residual } -> S32.
+// Iterations per pass of the WHILE body.  Each pass of the loop costs about 4 us more than a plain kernel
+// boundary (measured with per-kernel timestamps inside the graph, 27-point 128^3), so the body holds
+// several iterations; the kernels of the iterations after the one that stops return at once (one pass
+// of a few empty kernels, at the end of the solve).
+constexpr int kGraphUnroll = 4;
+
+// Graph: init kernels -> WHILE(loop) { kGraphUnroll iterations }.  A mixed iteration is
+// A32 -> B32 -> IF(ru) { flush, f64 SpMV, residual } -> S32, each IF with its own condition handle.
 int build_graph(dimgpu_cg_solver* s) {
     cudaGraph_t g = nullptr;
     DG_CUDA(cudaGraphCreate(&g, 0));
@@ -693,36 +699,44 @@ int build_graph(dimgpu_cg_solver* s) {
         if ((rc = add_conditional(g, leaves, c.loop, cudaGraphCondTypeWhile, &wnode, &body)) != DIMGPU_OK)
             break;
         if (!mixed(s)) {
-            rc = capture_into(cap, body, {}, nullptr, [&] { return enqueue_iteration(s, c, cap); });
+            rc = capture_into(cap, body, {}, nullptr, [&]() -> int {
+                for (int u = 0; u < kGraphUnroll; ++u)
+                    DG_CHECK(enqueue_iteration(s, c, cap));
+                return DIMGPU_OK;
+            });
             if (rc != DIMGPU_OK)
                 break;
         } else {
-            if ((e = cudaGraphConditionalHandleCreate(&c.ru, body, 0, 0)) != cudaSuccess) {
-                rc = cuda_fail(e, "cudaGraphConditionalHandleCreate (reliable update)");
-                break;
+            std::vector<cudaGraphNode_t> prev;  // leaves of the previous iteration in the body
+            for (int u = 0; u < kGraphUnroll && rc == DIMGPU_OK; ++u) {
+                vec_ctx cu = c;
+                if ((e = cudaGraphConditionalHandleCreate(&cu.ru, body, 0, 0)) != cudaSuccess) {
+                    rc = cuda_fail(e, "cudaGraphConditionalHandleCreate (reliable update)");
+                    break;
+                }
+                cu.has_ru = 1;
+                std::vector<cudaGraphNode_t> ab;
+                rc = capture_into(cap, body, prev, &ab, [&]() -> int {
+                    DG_CHECK(launch_spmv_f32(s->m, s->s32, s->As32, &s->cal, cg_epilogue(s), cap));
+                    k_update_r_mixed<<<s->grid, kVecThreads, 0, cap>>>(s->As32, s->r32, s->s32, s->y32, s->n, cu);
+                    DG_CUDA(cudaGetLastError());
+                    return DIMGPU_OK;
+                });
+                if (rc != DIMGPU_OK)
+                    break;
+                cudaGraphNode_t inode;
+                cudaGraph_t ibody;
+                if ((rc = add_conditional(body, ab, cu.ru, cudaGraphCondTypeIf, &inode, &ibody)) != DIMGPU_OK)
+                    break;
+                if ((rc = capture_into(cap, ibody, {}, nullptr,
+                                       [&] { return enqueue_reliable_update(s, cu, cap); })) != DIMGPU_OK)
+                    break;
+                rc = capture_into(cap, body, {inode}, &prev, [&]() -> int {
+                    k_update_s_mixed<<<s->grid, kVecThreads, 0, cap>>>(s->s32, s->r32, s->n, s->st);
+                    DG_CUDA(cudaGetLastError());
+                    return DIMGPU_OK;
+                });
             }
-            c.has_ru = 1;
-            std::vector<cudaGraphNode_t> ab;
-            rc = capture_into(cap, body, {}, &ab, [&]() -> int {
-                DG_CHECK(launch_spmv_f32(s->m, s->s32, s->As32, &s->cal, cg_epilogue(s), cap));
-                k_update_r_mixed<<<s->grid, kVecThreads, 0, cap>>>(s->As32, s->r32, s->s32, s->y32, s->n, c);
-                DG_CUDA(cudaGetLastError());
-                return DIMGPU_OK;
-            });
-            if (rc != DIMGPU_OK)
-                break;
-            cudaGraphNode_t inode;
-            cudaGraph_t ibody;
-            if ((rc = add_conditional(body, ab, c.ru, cudaGraphCondTypeIf, &inode, &ibody)) != DIMGPU_OK)
-                break;
-            if ((rc = capture_into(cap, ibody, {}, nullptr, [&] { return enqueue_reliable_update(s, c, cap); })) !=
-                DIMGPU_OK)
-                break;
-            rc = capture_into(cap, body, {inode}, nullptr, [&]() -> int {
-                k_update_s_mixed<<<s->grid, kVecThreads, 0, cap>>>(s->s32, s->r32, s->n, s->st);
-                DG_CUDA(cudaGetLastError());
-                return DIMGPU_OK;
-            });
             if (rc != DIMGPU_OK)
                 break;
         }
