@@ -451,7 +451,7 @@ int ensure_vals32(const dimgpu_csr5* cm, cudaStream_t s) {
     }
     m->vals32 = v;
     m->device_bytes += m->nnz * sizeof(float);
-    return DIMGPU_OK;
+    return autotune_f32(m, s);
 }
 
 }  // namespace dimgpu

@@ -88,9 +88,10 @@ struct dimgpu_csr5 {
     void* spmm_sc = nullptr;     // the handle's own SpMM scratch (dimgpu::spmm_scratch), built on first use
     dimgpu_csr5* transposed = nullptr;  // A^T, built on first transpose use
     int keep_in_l2 = 0;        // matrix + CG vectors fit in L2: stream the matrix without evict-first
-    int x_mode = 0;            // how SpMV gathers x (spmv_tile.cuh: kXReadOnly or kXStream), autotuned
-    dimgpu::spmv_plan plan;    // f64 SpMV launch
-    dimgpu::spmv_plan plan32;  // f32 SpMV launch (more warps per CTA)
+    int x_mode = 0;            // how the f64 SpMV gathers x (spmv_tile.cuh: kXReadOnly or kXStream), autotuned
+    int x_mode32 = 0;          // the same for the f32 SpMV (tuned when the f32 values are made)
+    dimgpu::spmv_plan plan;    // f64 SpMV launch (warps per CTA autotuned at conversion)
+    dimgpu::spmv_plan plan32;  // f32 SpMV launch (more warps per CTA; tuned with the f32 values)
     dimgpu_calibrator* own_cal = nullptr;
 };
 
@@ -124,6 +125,7 @@ int launch_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calib
                     const spmv_epilogue& ep, cudaStream_t stream);
 int check_status(dimgpu_calibrator* cal, cudaStream_t stream);
 int autotune_gathers(dimgpu_csr5* m, cudaStream_t stream);
+int autotune_f32(dimgpu_csr5* m, cudaStream_t stream);
 int vec_fill(uint64_t n, double v, double* y, cudaStream_t stream);
 
 // spmm.cu: CSR5 SpMM (lanes = right-hand sides, one pass takes k <= 32 columns)

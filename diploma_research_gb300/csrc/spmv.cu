@@ -38,6 +38,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <vector>
 #include <mutex>
 
 #include "common.cuh"
@@ -343,7 +344,7 @@ int launch_cfg(const dimgpu_csr5* m, const VT* vals, const VT* x, VT* y, dimgpu_
     p.rr = ep.rr;
     p.alpha_out = ep.alpha_out;
     p.halt = ep.halt;
-    if (m->x_mode == kXStream)
+    if ((sizeof(VT) == 8 ? m->x_mode : m->x_mode32) == kXStream)
         k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXStream><<<pl.grid, WPC * 32, smem, stream>>>(p);
     else
         k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXReadOnly><<<pl.grid, WPC * 32, smem, stream>>>(p);
@@ -351,8 +352,14 @@ int launch_cfg(const dimgpu_csr5* m, const VT* vals, const VT* x, VT* y, dimgpu_
     return DIMGPU_OK;
 }
 
-constexpr int kWPC = 16;    // f64: 16 warps x 2 stages x 6.3 KB per SM (register-limited)
-constexpr int kWPC32 = 24;  // f32: 24 warps x 2 stages x 4.2 KB per SM
+// Warps per CTA (one CTA per SM).  Fewer warps hold less shared memory, which leaves more of the SM's
+// 256 KB to L1: gathers that revisit a small part of x (the hub columns of a power-law matrix) then hit
+// L1, and that can outweigh the latency hiding of more warps.  Each matrix gets the faster of the two
+// per precision, timed at conversion (f64) and when its f32 values are made (f32).
+constexpr int kWPC = 16;      // f64: 16 warps x 2 stages x 6.3 KB per SM (register-limited)
+constexpr int kWPCL1 = 12;    // f64, L1-leaning: 12 warps, 151 KB of stages
+constexpr int kWPC32 = 24;    // f32: 24 warps x 2 stages x 4.2 KB per SM
+constexpr int kWPC32L1 = 20;  // f32, L1-leaning: 20 warps, 168 KB of stages
 constexpr int kStages = 2;
 
 template <typename VT, int SIGMA, int WPC, int STAGES, bool DOT>
@@ -376,8 +383,12 @@ int prepare_spmv_kernels() {
         return DIMGPU_OK;
     DG_CUDA((set_smem_attr<double, 16, kWPC, kStages, false>()));
     DG_CUDA((set_smem_attr<double, 16, kWPC, kStages, true>()));
+    DG_CUDA((set_smem_attr<double, 16, kWPCL1, kStages, false>()));
+    DG_CUDA((set_smem_attr<double, 16, kWPCL1, kStages, true>()));
     DG_CUDA((set_smem_attr<float, 16, kWPC32, kStages, false>()));
     DG_CUDA((set_smem_attr<float, 16, kWPC32, kStages, true>()));
+    DG_CUDA((set_smem_attr<float, 16, kWPC32L1, kStages, false>()));
+    DG_CUDA((set_smem_attr<float, 16, kWPC32L1, kStages, true>()));
     done = 1;
     return DIMGPU_OK;
 }
@@ -440,6 +451,9 @@ int launch_spmv_f64(const dimgpu_csr5* m, const double* x, double* y, dimgpu_cal
     const bool dot = ep.dot_out || ep.alpha_out;
     switch (m->sigma) {
     case 16:
+        if (m->plan.warps_per_cta == kWPCL1)
+            return dot ? launch_cfg<double, 16, kWPCL1, kStages, true>(m, m->vals, x, y, cal, ep, stream)
+                       : launch_cfg<double, 16, kWPCL1, kStages, false>(m, m->vals, x, y, cal, ep, stream);
         return dot ? launch_cfg<double, 16, kWPC, kStages, true>(m, m->vals, x, y, cal, ep, stream)
                    : launch_cfg<double, 16, kWPC, kStages, false>(m, m->vals, x, y, cal, ep, stream);
     default:
@@ -455,6 +469,9 @@ int launch_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calib
     const bool dot = ep.dot_out || ep.alpha_out;
     switch (m->sigma) {
     case 16:
+        if (m->plan32.warps_per_cta == kWPC32L1)
+            return dot ? launch_cfg<float, 16, kWPC32L1, kStages, true>(m, m->vals32, x, y, cal, ep, stream)
+                       : launch_cfg<float, 16, kWPC32L1, kStages, false>(m, m->vals32, x, y, cal, ep, stream);
         return dot ? launch_cfg<float, 16, kWPC32, kStages, true>(m, m->vals32, x, y, cal, ep, stream)
                    : launch_cfg<float, 16, kWPC32, kStages, false>(m, m->vals32, x, y, cal, ep, stream);
     default:
@@ -462,43 +479,96 @@ int launch_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calib
     }
 }
 
-// Chooses how the x gathers load (kept in L1, or streamed past it) by timing both on this matrix: an
-// f64 SpMV of x = 1, the faster of two timed launches per mode.  Small matrices keep the default.
-int autotune_gathers(dimgpu_csr5* m, cudaStream_t stream) {
-    m->x_mode = kXReadOnly;
-    if (m->tile_count < 4096 || m->rows == 0 || m->cols == 0)
-        return DIMGPU_OK;
-    double *x = nullptr, *y = nullptr;
+// Times the SpMV of this matrix (x = 1) in each launch configuration `set(i)` installs, the faster of two
+// timed launches after one untimed; returns the index of the fastest, which must beat configuration 0
+// (the default) by 3 % to be chosen.
+template <typename VT, typename Set>
+int time_configs(dimgpu_csr5* m, int nconf, Set set, cudaStream_t stream, int* chosen) {
+    *chosen = 0;
+    VT *x = nullptr, *y = nullptr;
     DG_CHECK(dev_alloc_n(&x, m->cols));
     int rc = dev_alloc_n(&y, m->rows);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    float best[2] = {1e30f, 1e30f};
+    float best[4] = {1e30f, 1e30f, 1e30f, 1e30f};
     if (rc == DIMGPU_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
         rc = cuda_fail(cudaGetLastError(), "cudaEventCreate");
-    if (rc == DIMGPU_OK)
-        rc = vec_fill(m->cols, 1.0, x, stream);
-    for (int mode = 0; mode < 2 && rc == DIMGPU_OK; ++mode) {
-        m->x_mode = mode == 0 ? kXReadOnly : kXStream;
+    if (rc == DIMGPU_OK) {
+        if constexpr (sizeof(VT) == 8) {
+            rc = vec_fill(m->cols, 1.0, x, stream);
+        } else {
+            std::vector<float> ones(m->cols, 1.0f);
+            if (cudaMemcpyAsync(x, ones.data(), sizeof(float) * m->cols, cudaMemcpyHostToDevice, stream) !=
+                    cudaSuccess ||
+                cudaStreamSynchronize(stream) != cudaSuccess)
+                rc = cuda_fail(cudaGetLastError(), "x = 1");
+        }
+    }
+    for (int i = 0; i < nconf && i < 4 && rc == DIMGPU_OK; ++i) {
+        set(i);
         for (int rep = 0; rep < 3 && rc == DIMGPU_OK; ++rep) {
             cudaEventRecord(e0, stream);
-            rc = launch_spmv_f64(m, x, y, m->own_cal, spmv_epilogue{}, stream);
+            if constexpr (sizeof(VT) == 8)
+                rc = launch_spmv_f64(m, x, y, m->own_cal, spmv_epilogue{}, stream);
+            else
+                rc = launch_spmv_f32(m, x, y, m->own_cal, spmv_epilogue{}, stream);
             cudaEventRecord(e1, stream);
             if (rc == DIMGPU_OK && cudaEventSynchronize(e1) == cudaSuccess && rep > 0) {
                 float ms = 0;
                 cudaEventElapsedTime(&ms, e0, e1);
-                best[mode] = std::min(best[mode], ms);
+                best[i] = std::min(best[i], ms);
             }
         }
     }
     if (rc == DIMGPU_OK)
         rc = check_status(m->own_cal, stream);
-    m->x_mode = best[1] < 0.97f * best[0] ? kXStream : kXReadOnly;
+    int b = 0;
+    for (int i = 1; i < nconf && i < 4; ++i)
+        if (best[i] < best[b])
+            b = i;
+    *chosen = (b != 0 && best[b] < 0.97f * best[0]) ? b : 0;
     if (e0)
         cudaEventDestroy(e0);
     if (e1)
         cudaEventDestroy(e1);
     dev_free(x);
     dev_free(y);
+    return rc;
+}
+
+// Chooses the f64 SpMV's launch for this matrix by timing: warps per CTA (16, or 12 to leave more L1)
+// times how the x gathers load (kept in L1, or streamed past it).  Small matrices keep the default.
+int autotune_gathers(dimgpu_csr5* m, cudaStream_t stream) {
+    m->x_mode = kXReadOnly;
+    if (m->tile_count < 4096 || m->rows == 0 || m->cols == 0)
+        return DIMGPU_OK;
+    const int sms = device_sm_count(m->device);
+    const int wpc[2] = {kWPC, kWPCL1};
+    const int mode[2] = {kXReadOnly, kXStream};
+    auto set = [&](int i) {
+        m->plan = make_spmv_plan(m->tile_count, sms, wpc[i / 2]);
+        m->x_mode = mode[i % 2];
+    };
+    int c = 0;
+    const int rc = time_configs<double>(m, 4, set, stream, &c);
+    set(rc == DIMGPU_OK ? c : 0);
+    return rc;
+}
+
+// The same for the f32 SpMV (24 or 20 warps per CTA), run once, when the f32 values are made.
+int autotune_f32(dimgpu_csr5* m, cudaStream_t stream) {
+    m->x_mode32 = m->x_mode;
+    if (m->layout != kLayoutDevice || m->sigma != 16 || m->tile_count < 4096 || m->rows == 0 || m->cols == 0)
+        return DIMGPU_OK;
+    const int sms = device_sm_count(m->device);
+    const int wpc[2] = {kWPC32, kWPC32L1};
+    const int mode[2] = {kXReadOnly, kXStream};
+    auto set = [&](int i) {
+        m->plan32 = make_spmv_plan(m->tile_count, sms, wpc[i / 2]);
+        m->x_mode32 = mode[i % 2];
+    };
+    int c = 0;
+    const int rc = time_configs<float>(m, 4, set, stream, &c);
+    set(rc == DIMGPU_OK ? c : 0);
     return rc;
 }
 
