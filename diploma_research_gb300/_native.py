@@ -102,6 +102,8 @@ _SIGNATURES = {
     "dimgpu_csr5_spmv": [_vp, _vp, _vp, _vp, _vp],
     "dimgpu_csr5_spmv_host": [_vp, _vp, _vp],
     "dimgpu_csr5_spmv_dot": [_vp, _vp, _vp, _vp, _vp, _vp],
+    "dimgpu_csr5_get_spmv_launch": [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int)],
+    "dimgpu_csr5_set_spmv_launch": [_vp, ctypes.c_int, ctypes.c_uint32, ctypes.c_int],
     "dimgpu_csr5_spmv_f32": [_vp, _vp, _vp, _vp, _vp],
     "dimgpu_csr5_spmm": [_vp, _u32, _vp, _u64, _vp, _u64, _vp],
     "dimgpu_csr5_spmm_f32": [_vp, _u32, _vp, _u64, _vp, _u64, _vp],

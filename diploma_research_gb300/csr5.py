@@ -188,6 +188,21 @@ class csr5:
                 body((row, int(c[k])), float(v[k]))
 
     # ---- SpMV -----------------------------------------------------------------------------------
+    _GATHER = {"l1": 0, "stream": 1}
+
+    def spmv_launch(self, f32: bool = False) -> tuple[int, str]:
+        """(warps per CTA, "l1" | "stream") of this matrix's SpMV launch, as the library chose it by timing
+        (f32=True: the f32 product's, making its values first if needed)."""
+        w, g = ctypes.c_uint32(), ctypes.c_int()
+        N.check(N.lib().dimgpu_csr5_get_spmv_launch(self._h, int(f32), ctypes.byref(w), ctypes.byref(g)))
+        return int(w.value), "stream" if g.value == 1 else "l1"
+
+    def set_spmv_launch(self, warps_per_cta: int, gather: str = "l1", f32: bool = False) -> None:
+        """Pins the launch (f64: 16 or 12 warps per CTA; f32: 24 or 20; gather "l1" or "stream")."""
+        if gather not in self._GATHER:
+            raise ValueError(f"gather must be one of {sorted(self._GATHER)}")
+        N.check(N.lib().dimgpu_csr5_set_spmv_launch(self._h, int(f32), int(warps_per_cta), self._GATHER[gather]))
+
     def spmv(self, data, y=None, calibrator: calibrator_t | None = None, stream=None):
         """y := A x (csr5.h:818-829).  ``data`` is an spmv_data_t or x (then pass y)."""
         if isinstance(data, spmv_data_t):

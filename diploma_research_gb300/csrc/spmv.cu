@@ -421,7 +421,12 @@ spmv_plan make_spmv_plan32(uint64_t tiles, int sms) { return make_spmv_plan(tile
 
 int calibrator_init(dimgpu_calibrator* c, const dimgpu_csr5* m) {
     cudaGetDevice(&c->device);
-    c->nslots = std::max<uint32_t>(std::max(m->plan.nwarps, m->plan32.nwarps), 1);
+    // slots for every launch configuration the matrix may use, so that pinning another keeps it valid
+    const int sms = device_sm_count(m->device);
+    uint32_t most = std::max(m->plan.nwarps, m->plan32.nwarps);
+    for (int w : {kWPC, kWPCL1, kWPC32, kWPC32L1})
+        most = std::max(most, make_spmv_plan(m->tile_count, sms, w).nwarps);
+    c->nslots = std::max<uint32_t>(most, 1);
     DG_CHECK(dev_alloc_n(&c->cal_val, c->nslots));
     DG_CHECK(dev_alloc_n(&c->cal_row, c->nslots));
     DG_CHECK(dev_alloc_n(&c->dot_part, c->nslots + 1));
@@ -637,6 +642,43 @@ int static_scratch_on(int device, unsigned char** out) {
 
 }  // namespace
 }  // namespace dimgpu
+
+extern "C" int dimgpu_csr5_get_spmv_launch(const dimgpu_csr5* m, int f32, uint32_t* warps_per_cta, int* gather) {
+    using namespace dimgpu;
+    if (!m || !warps_per_cta || !gather)
+        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (f32)
+        DG_CHECK(ensure_vals32(m, nullptr));
+    *warps_per_cta = (uint32_t)(f32 ? m->plan32 : m->plan).warps_per_cta;
+    *gather = (f32 ? m->x_mode32 : m->x_mode) == kXStream ? DIMGPU_GATHER_STREAM : DIMGPU_GATHER_L1;
+    return DIMGPU_OK;
+}
+
+extern "C" int dimgpu_csr5_set_spmv_launch(dimgpu_csr5* m, int f32, uint32_t warps_per_cta, int gather) {
+    using namespace dimgpu;
+    if (!m)
+        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "NULL matrix");
+    if (m->layout != kLayoutDevice || m->sigma != 16)
+        return fail(DIMGPU_ERR_UNSUPPORTED, "the SpMV launch is chosen only for the 32-lane device layout at sigma 16");
+    if (gather != DIMGPU_GATHER_L1 && gather != DIMGPU_GATHER_STREAM)
+        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "gather mode %d", gather);
+    const bool ok = f32 ? (warps_per_cta == (uint32_t)kWPC32 || warps_per_cta == (uint32_t)kWPC32L1)
+                        : (warps_per_cta == (uint32_t)kWPC || warps_per_cta == (uint32_t)kWPCL1);
+    if (!ok)
+        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "%u warps per CTA is not an %s SpMV launch (%d or %d)", warps_per_cta,
+                    f32 ? "f32" : "f64", f32 ? kWPC32 : kWPC, f32 ? kWPC32L1 : kWPCL1);
+    const spmv_plan pl = make_spmv_plan(m->tile_count, device_sm_count(m->device), (int)warps_per_cta);
+    const int mode = gather == DIMGPU_GATHER_STREAM ? kXStream : kXReadOnly;
+    if (f32) {
+        DG_CHECK(ensure_vals32(m, nullptr));  // makes (and tunes) the f32 values first, then the pin holds
+        m->plan32 = pl;
+        m->x_mode32 = mode;
+    } else {
+        m->plan = pl;
+        m->x_mode = mode;
+    }
+    return DIMGPU_OK;
+}
 
 extern "C" int dimgpu_csr5_spmv_static_scratch(const dimgpu_csr5* m, const double* x, double* y, void* stream) {
     using namespace dimgpu;

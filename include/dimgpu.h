@@ -116,6 +116,19 @@ DIMGPU_API int dimgpu_csr5_spmv_host(const dimgpu_csr5* m, const double* x_host,
  * The first call builds an f32 copy of the values inside the handle. */
 DIMGPU_API int dimgpu_csr5_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calibrator* cal, void* stream);
 
+/* The SpMV launch configuration of this matrix: warps per CTA and how the x gathers load
+ * (DIMGPU_GATHER_L1: kept in L1; DIMGPU_GATHER_STREAM: past L1).  The library chooses them by timing,
+ * at conversion for the f64 product and when the f32 values are made for the f32 product (f32 != 0;
+ * get makes them if needed).  Fewer warps leave more of the SM to L1, which helps matrices whose
+ * gathers revisit a small part of x.  No reference counterpart (the reference's OpenMP SpMV has no
+ * launch configuration). */
+#define DIMGPU_GATHER_L1 0
+#define DIMGPU_GATHER_STREAM 1
+DIMGPU_API int dimgpu_csr5_get_spmv_launch(const dimgpu_csr5* m, int f32, uint32_t* warps_per_cta, int* gather);
+/* Pins it (f64: 16 or 12 warps per CTA; f32: 24 or 20), e.g. for reproducible timings.  Calibrators
+ * made before stay valid.  Must not overlap with products on the matrix in flight. */
+DIMGPU_API int dimgpu_csr5_set_spmv_launch(dimgpu_csr5* m, int f32, uint32_t warps_per_cta, int gather);
+
 /* y := A x like dimgpu_csr5_spmv, but neither this call nor the library allocates anything: the
  * scratch (per-warp row fragments, completion ticket, status word) is a fixed array of 98,816 bytes
  * compiled into the library, present on every GPU that loads it until the process exits.  It has no

@@ -187,3 +187,90 @@ def test_power_law_full_size(native, torch_cuda):
     m = power_law()
     rng = np.random.default_rng(12)
     _check(torch_cuda, m, rng.uniform(-1, 1, m.dimensions.cols))
+
+
+def _launch_matrices(rng):
+    yield random_csr(rng, 9000, 9000, 12.0, empty_frac=0.1, long_rows=4, long_len=(600, 6000))
+    yield csr_from_lengths([3] * 10000 + [20000] + [5] * 13999, 24000, rng)  # one row across many warp runs
+    yield random_csr(rng, 3000, 3000, 2.0)
+
+
+@pytest.mark.parametrize("warps,gather", [(16, "l1"), (16, "stream"), (12, "l1"), (12, "stream")])
+def test_every_f64_launch_configuration(native, torch_cuda, warps, gather):
+    """Each f64 launch the per-matrix timing may choose, pinned: the product, the product with the fused
+    dot, and a CG solve."""
+    import ctypes
+
+    from diploma_research_gb300 import _native as N
+    from diploma_research_gb300.cg import cg
+
+    torch = torch_cuda
+    rng = np.random.default_rng(70 + warps)
+    for m in _launch_matrices(rng):
+        n = m.dimensions.rows
+        A = csr5.from_csr(m)
+        A.set_spmv_launch(warps, gather)
+        assert A.spmv_launch() == (warps, gather)
+        x = rng.uniform(-1, 1, n)
+        xd = torch.tensor(x, device="cuda", dtype=torch.float64)
+        yd = torch.full((n,), float("nan"), device="cuda", dtype=torch.float64)
+        dot = torch.zeros(1, device="cuda", dtype=torch.float64)
+        N.check(native.dimgpu_csr5_spmv_dot(A._h, xd.data_ptr(), yd.data_ptr(), dot.data_ptr(), None, None))
+        torch.cuda.synchronize()
+        y_ref, ax = _refs(m, x)
+        assert_spmv_close(yd.cpu().numpy(), y_ref, ax, SPMV_RTOL_F64)
+        assert abs(float(dot.item()) - float(np.dot(x, y_ref))) <= 1e-12 * float(np.dot(np.abs(x), ax))
+        yp = _gpu_spmv(torch, A, x)
+        assert_spmv_close(yp, y_ref, ax, SPMV_RTOL_F64)
+    # a CG solve on this launch (its SpMV with the fused dot inside the graph)
+    from diploma_research_gb300.generators import laplacian_2d_5pt
+
+    L = laplacian_2d_5pt(64)
+    A = csr5.from_csr(L)
+    A.set_spmv_launch(warps, gather)
+    b = oracle.csr_spmv(L.dimensions.rows, L.row_start_offsets, L.col_indices, L.values,
+                        rng.uniform(-1, 1, L.dimensions.rows))
+    _, res = cg(A, b, tol=1e-10)
+    assert res.converged and res.rel_residual <= 1e-10
+
+
+@pytest.mark.parametrize("warps,gather", [(24, "l1"), (24, "stream"), (20, "l1"), (20, "stream")])
+def test_every_f32_launch_configuration(native, torch_cuda, warps, gather):
+    """Each f32 launch, pinned: the f32 product, and a mixed-precision CG solve (its f32 product with the
+    fused dot)."""
+    from diploma_research_gb300.cg import cg
+
+    torch = torch_cuda
+    rng = np.random.default_rng(80 + warps)
+    for m in _launch_matrices(rng):
+        n = m.dimensions.rows
+        A = csr5.from_csr(m)
+        A.set_spmv_launch(warps, gather, f32=True)
+        assert A.spmv_launch(f32=True) == (warps, gather)
+        x = rng.uniform(-1, 1, n)
+        xd = torch.tensor(x, device="cuda", dtype=torch.float32)
+        yd = torch.full((n,), float("nan"), device="cuda", dtype=torch.float32)
+        A.spmv(xd, yd)
+        torch.cuda.synchronize()
+        y_ref, ax = _refs(m, x.astype(np.float32).astype(np.float64))
+        assert_spmv_close(yd.cpu().numpy().astype(np.float64), y_ref, ax, SPMV_RTOL_F32 * 50)
+    from diploma_research_gb300.generators import laplacian_2d_5pt
+
+    L = laplacian_2d_5pt(64)
+    A = csr5.from_csr(L)
+    A.set_spmv_launch(warps, gather, f32=True)
+    b = oracle.csr_spmv(L.dimensions.rows, L.row_start_offsets, L.col_indices, L.values,
+                        rng.uniform(-1, 1, L.dimensions.rows))
+    _, res = cg(A, b, tol=1e-10, precision="mixed")
+    assert res.converged and res.rel_residual <= 1e-10
+
+
+def test_launch_configuration_errors(native, torch_cuda):
+    A = csr5.from_csr(random_csr(np.random.default_rng(1), 500, 500, 5.0))
+    with pytest.raises(ValueError):
+        A.set_spmv_launch(20)  # an f32 launch, not an f64 one
+    with pytest.raises(ValueError):
+        A.set_spmv_launch(16, f32=True)
+    with pytest.raises(ValueError):
+        A.set_spmv_launch(16, gather="texture")
+    assert A.spmv_launch() == (16, "l1")  # small matrices keep the default
