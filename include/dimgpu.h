@@ -113,7 +113,9 @@ DIMGPU_API int dimgpu_csr5_spmv_dot(const dimgpu_csr5* m, const double* x, doubl
 DIMGPU_API int dimgpu_csr5_spmv_host(const dimgpu_csr5* m, const double* x_host, double* y_host);
 
 /* y := A x with f32 values, vectors and row sums (the inner kernel of the mixed-precision CG).
- * The first call builds an f32 copy of the values inside the handle. */
+ * The first f32 use of a matrix (this call, an f32 SpMM, a mixed-precision solver, or
+ * dimgpu_csr5_get_spmv_launch with f32) builds an f32 copy of the values inside the handle and times
+ * the f32 launch configurations; it synchronizes, so make it outside stream capture. */
 DIMGPU_API int dimgpu_csr5_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calibrator* cal, void* stream);
 
 /* The SpMV launch configuration of this matrix: warps per CTA and how the x gathers load
