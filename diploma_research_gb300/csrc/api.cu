@@ -142,6 +142,8 @@ static void destroy_matrix(dimgpu_csr5* m) {
     dev_free(m->row_ptr);
     dev_free(m->vals);
     dev_free(m->col);
+    dev_free(m->col16);
+    dev_free(m->col_base);
     dev_free(m->tile_ptr);
     dev_free(m->tile_desc);
     dev_free(m->tdo_ptr);
@@ -246,6 +248,7 @@ int dimgpu_csr5_from_csr(uint32_t rows, uint32_t cols, uint64_t nnz, const uint3
         }
         if ((rc = prepare_spmv_kernels()) != DIMGPU_OK) break;
         if ((rc = convert_csr5(m, d_rp, d_ci, d_v, s)) != DIMGPU_OK) break;
+        if (m->layout == kLayoutDevice && m->sigma == 16 && (rc = build_col16(m, s)) != DIMGPU_OK) break;
         m->plan = make_spmv_plan(m->tile_count, device_sm_count(m->device), 16);
         {
             // A matrix that fits in L2 together with the CG vectors (six f64 n-vectors) is better left

@@ -313,6 +313,36 @@ __global__ void k_vals32_device(const double* vals, float* out, const uint32_t* 
     }
 }
 
+// Per full tile (one warp each): the smallest column of the tile into base[t]; sets *wide when the tile's
+// columns span 2^16 or more.
+__global__ void k_col_base(const uint32_t* col, uint64_t T, uint32_t ts, uint32_t* base, uint32_t* wide) {
+    const unsigned lane = threadIdx.x & 31u;
+    for (uint64_t t = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32; t < T;
+         t += (uint64_t)gridDim.x * blockDim.x / 32) {
+        uint32_t lo = 0xFFFFFFFFu, hi = 0u;
+        for (uint32_t k = lane; k < ts; k += 32) {
+            const uint32_t c = col[t * ts + k];
+            lo = min(lo, c);
+            hi = max(hi, c);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        if (lane == 0) {
+            base[t] = lo;
+            if (hi - lo > 0xFFFFu)
+                atomicOr(wide, 1u);
+        }
+    }
+}
+
+// col16[e] = col[e] - base[tile of e] for the full tiles.
+__global__ void k_col16(const uint32_t* col, const uint32_t* base, uint64_t n, uint32_t ts, uint16_t* col16) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < n; e += (uint64_t)gridDim.x * blockDim.x)
+        col16[e] = (uint16_t)(col[e] - base[e / ts]);
+}
+
 inline unsigned grid_for(uint64_t n, int threads = 256) {
     uint64_t b = (n + threads - 1) / threads;
     if (b == 0)
@@ -429,6 +459,41 @@ int convert_csr5(dimgpu_csr5* m, const uint32_t* d_row_ptr, const uint32_t* d_co
                           T * omega * m->desc_word_bytes + nnz * (sizeof(double) + sizeof(uint32_t));
     }
     return rc;
+}
+
+// The 16-bit column offsets of the device layout, when every full tile's columns fit (see internal.hpp).
+int build_col16(dimgpu_csr5* m, cudaStream_t s) {
+    const uint64_t T = m->tile_count, ts = (uint64_t)m->sigma * m->omega;
+    if (m->layout != kLayoutDevice || T == 0)
+        return DIMGPU_OK;
+    uint32_t *base = nullptr, *wide = nullptr;
+    DG_CHECK(dev_alloc_n(&base, T));
+    int rc = dev_alloc_n(&wide, 1);
+    uint32_t w = 1;
+    if (rc == DIMGPU_OK && cudaMemsetAsync(wide, 0, sizeof(uint32_t), s) != cudaSuccess)
+        rc = cuda_fail(cudaGetLastError(), "memset");
+    if (rc == DIMGPU_OK) {
+        k_col_base<<<grid_for(T * 32), 256, 0, s>>>(m->col, T, (uint32_t)ts, base, wide);
+        if (cudaMemcpyAsync(&w, wide, sizeof(w), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            rc = cuda_fail(cudaGetLastError(), "column span of the tiles");
+    }
+    dev_free(wide);
+    uint16_t* c16 = nullptr;
+    if (rc == DIMGPU_OK && w == 0 && (rc = dev_alloc_n(&c16, T * ts)) == DIMGPU_OK) {
+        k_col16<<<grid_for(T * ts), 256, 0, s>>>(m->col, base, T * ts, (uint32_t)ts, c16);
+        if (cudaStreamSynchronize(s) != cudaSuccess)
+            rc = cuda_fail(cudaGetLastError(), "16-bit column offsets");
+    }
+    if (rc != DIMGPU_OK || w != 0) {
+        dev_free(base);
+        dev_free(c16);
+        return rc;
+    }
+    m->col16 = c16;
+    m->col_base = base;
+    m->device_bytes += T * ts * sizeof(uint16_t) + T * sizeof(uint32_t);
+    return DIMGPU_OK;
 }
 
 int ensure_vals32(const dimgpu_csr5* cm, cudaStream_t s) {

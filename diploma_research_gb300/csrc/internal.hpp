@@ -76,6 +76,11 @@ struct dimgpu_csr5 {
     uint32_t* row_ptr = nullptr;   // [rows+1]
     double* vals = nullptr;        // [nnz] re-ordered
     uint32_t* col = nullptr;       // [nnz] re-ordered
+    // Device layout only, when every full tile's columns span less than 2^16: each tile's column indices
+    // as u16 offsets from the tile's smallest column (same order as col), which the SpMV streams instead
+    // of col (2 bytes per non-zero fewer).  nullptr when some tile spans more.
+    uint16_t* col16 = nullptr;     // [T * sigma * omega]
+    uint32_t* col_base = nullptr;  // [T]
     uint32_t* tile_ptr = nullptr;  // [T+1]
     void* tile_desc = nullptr;     // [T*omega] words
     uint32_t* tdo_ptr = nullptr;   // [T+1]
@@ -101,6 +106,7 @@ namespace dimgpu {
 int convert_csr5(dimgpu_csr5* m, const uint32_t* d_row_ptr, const uint32_t* d_col, const double* d_vals,
                  cudaStream_t stream);
 int ensure_vals32(const dimgpu_csr5* m, cudaStream_t stream);
+int build_col16(dimgpu_csr5* m, cudaStream_t stream);
 
 // spmv.cu
 spmv_plan make_spmv_plan(uint64_t tiles, int sms, int warps_per_cta);

@@ -53,6 +53,8 @@ template <typename VT>
 struct spmv_params {
     const VT* vals;
     const uint32_t* col;
+    const uint16_t* col16;     // 16-bit column offsets of the full tiles (kernels with IDX16)
+    const uint32_t* col_base;  // [T] their bases
     const void* desc;
     const uint32_t* tile_ptr;
     const uint32_t* tdo_ptr;
@@ -104,9 +106,9 @@ __device__ VT close_row(const spmv_params<VT>& p, uint32_t run, uint32_t R, VT o
     return acc + own;
 }
 
-template <typename VT, int SIGMA, int WPC, int STAGES, bool DOT, int XM>
+template <typename VT, int SIGMA, int WPC, int STAGES, bool DOT, int XM, bool IDX16>
 __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
-    using G = tile_geom<VT, SIGMA>;
+    using G = tile_geom<VT, SIGMA, IDX16>;
     using Word = typename G::Word;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint32_t s_last, s_cta, s_epoch;
@@ -153,16 +155,24 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
             unsigned char* st = ring + (size_t)s * G::STAGE;
             mbar_arrive_expect_tx(&bars[s], G::STAGE);
             bulk_g2s(st, p.vals + t * G::TS, G::VBYTES, &bars[s], pol);
-            bulk_g2s(st + G::VBYTES, p.col + t * G::TS, G::CBYTES, &bars[s], pol);
+            if constexpr (IDX16)
+                bulk_g2s(st + G::VBYTES, p.col16 + t * G::TS, G::CBYTES, &bars[s], pol);
+            else
+                bulk_g2s(st + G::VBYTES, p.col + t * G::TS, G::CBYTES, &bars[s], pol);
             bulk_g2s(st + G::VBYTES + G::CBYTES, gdesc + t * 32, G::DBYTES, &bars[s], pol);
         };
         if (lane == 0)
             for (int s = 0; s < STAGES && t_begin + s < t_end; ++s)
                 issue(s, t_begin + s);
 
-        // tile_ptr runs two tiles ahead so that no tile waits on its load
+        // tile_ptr (and the column base) run two tiles ahead so that no tile waits on its load
         uint32_t raw_cur = __ldg(&p.tile_ptr[t_begin]);
         uint32_t raw_next = __ldg(&p.tile_ptr[t_begin + 1]);
+        uint32_t base_cur = 0, base_next = 0;
+        if constexpr (IDX16) {
+            base_cur = __ldg(&p.col_base[t_begin]);
+            base_next = (t_begin + 1 < t_end) ? __ldg(&p.col_base[t_begin + 1]) : 0u;
+        }
         uint64_t i = 0;
         bool failed = false;
         for (uint64_t t = t_begin; t < t_end; ++t, ++i) {
@@ -172,11 +182,17 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
             const uint32_t raw_n = raw_next;
             raw_cur = raw_next;
             raw_next = (t + 2 <= p.T) ? __ldg(&p.tile_ptr[t + 2]) : 0u;
+            const uint32_t base = base_cur;
+            if constexpr (IDX16) {
+                base_cur = base_next;
+                base_next = (t + 2 < t_end) ? __ldg(&p.col_base[t + 2]) : 0u;
+            }
             if (!mbar_wait_bounded(&bars[s], par, p.status)) {
                 failed = true;
                 break;
             }
-            process_tile<VT, SIGMA, DOT, XM>(io, ring + (size_t)s * G::STAGE, lane, t, raw, raw_n, pol_keep, ch);
+            process_tile<VT, SIGMA, DOT, XM, IDX16>(io, ring + (size_t)s * G::STAGE, lane, t, raw, raw_n, pol_keep, ch,
+                                                    base);
 
             __syncwarp();
             if (lane == 0 && t + STAGES < t_end) {
@@ -302,15 +318,15 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
     }
 }
 
-template <typename VT, int SIGMA, int WPC, int STAGES>
+template <typename VT, int SIGMA, int WPC, int STAGES, bool IDX16>
 constexpr size_t smem_bytes() {
-    return 128 * ((WPC * STAGES * 8 + 127) / 128) + (size_t)WPC * STAGES * tile_geom<VT, SIGMA>::STAGE;
+    return 128 * ((WPC * STAGES * 8 + 127) / 128) + (size_t)WPC * STAGES * tile_geom<VT, SIGMA, IDX16>::STAGE;
 }
 
-template <typename VT, int SIGMA, int WPC, int STAGES, bool DOT>
+template <typename VT, int SIGMA, int WPC, int STAGES, bool DOT, bool IDX16>
 int launch_cfg(const dimgpu_csr5* m, const VT* vals, const VT* x, VT* y, dimgpu_calibrator* cal,
                const spmv_epilogue& ep, cudaStream_t stream) {
-    constexpr size_t smem = smem_bytes<VT, SIGMA, WPC, STAGES>();
+    constexpr size_t smem = smem_bytes<VT, SIGMA, WPC, STAGES, IDX16>();
     const spmv_plan& pl = sizeof(VT) == 8 ? m->plan : m->plan32;
     if (pl.warps_per_cta != WPC)
         return fail(DIMGPU_ERR_UNSUPPORTED, "launch plan has %d warps per CTA, kernel %d", pl.warps_per_cta, WPC);
@@ -319,6 +335,8 @@ int launch_cfg(const dimgpu_csr5* m, const VT* vals, const VT* x, VT* y, dimgpu_
     spmv_params<VT> p;
     p.vals = vals;
     p.col = m->col;
+    p.col16 = m->col16;
+    p.col_base = m->col_base;
     p.desc = m->tile_desc;
     p.tile_ptr = m->tile_ptr;
     p.tdo_ptr = m->tdo_ptr;
@@ -345,9 +363,9 @@ int launch_cfg(const dimgpu_csr5* m, const VT* vals, const VT* x, VT* y, dimgpu_
     p.alpha_out = ep.alpha_out;
     p.halt = ep.halt;
     if ((sizeof(VT) == 8 ? m->x_mode : m->x_mode32) == kXStream)
-        k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXStream><<<pl.grid, WPC * 32, smem, stream>>>(p);
+        k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXStream, IDX16><<<pl.grid, WPC * 32, smem, stream>>>(p);
     else
-        k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXReadOnly><<<pl.grid, WPC * 32, smem, stream>>>(p);
+        k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXReadOnly, IDX16><<<pl.grid, WPC * 32, smem, stream>>>(p);
     DG_CUDA(cudaGetLastError());
     return DIMGPU_OK;
 }
@@ -364,13 +382,20 @@ constexpr int kStages = 2;
 
 template <typename VT, int SIGMA, int WPC, int STAGES, bool DOT>
 cudaError_t set_smem_attr() {
-    const int bytes = (int)smem_bytes<VT, SIGMA, WPC, STAGES>();
-    cudaError_t e = cudaFuncSetAttribute(k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXReadOnly>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e != cudaSuccess)
+    cudaError_t e;
+    const int bytes = (int)smem_bytes<VT, SIGMA, WPC, STAGES, false>();
+    if ((e = cudaFuncSetAttribute(k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXReadOnly, false>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess)
         return e;
-    return cudaFuncSetAttribute(k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXStream>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if ((e = cudaFuncSetAttribute(k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXStream, false>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess)
+        return e;
+    const int bytes16 = (int)smem_bytes<VT, SIGMA, WPC, STAGES, true>();
+    if ((e = cudaFuncSetAttribute(k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXReadOnly, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes16)) != cudaSuccess)
+        return e;
+    return cudaFuncSetAttribute(k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXStream, true>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, bytes16);
 }
 
 }  // namespace
@@ -449,6 +474,15 @@ void calibrator_release(dimgpu_calibrator* c) {
     c->cal_val = nullptr;
 }
 
+// The launch with 16-bit column offsets when the matrix has them, 32-bit indices otherwise.
+template <typename VT, int SIGMA, int WPC, int STAGES, bool DOT>
+int launch_idx(const dimgpu_csr5* m, const VT* vals, const VT* x, VT* y, dimgpu_calibrator* cal,
+               const spmv_epilogue& ep, cudaStream_t stream) {
+    if (m->col16)
+        return launch_cfg<VT, SIGMA, WPC, STAGES, DOT, true>(m, vals, x, y, cal, ep, stream);
+    return launch_cfg<VT, SIGMA, WPC, STAGES, DOT, false>(m, vals, x, y, cal, ep, stream);
+}
+
 int launch_spmv_f64(const dimgpu_csr5* m, const double* x, double* y, dimgpu_calibrator* cal,
                     const spmv_epilogue& ep, cudaStream_t stream) {
     if (m->layout != kLayoutDevice || m->omega != 32)
@@ -457,10 +491,10 @@ int launch_spmv_f64(const dimgpu_csr5* m, const double* x, double* y, dimgpu_cal
     switch (m->sigma) {
     case 16:
         if (m->plan.warps_per_cta == kWPCL1)
-            return dot ? launch_cfg<double, 16, kWPCL1, kStages, true>(m, m->vals, x, y, cal, ep, stream)
-                       : launch_cfg<double, 16, kWPCL1, kStages, false>(m, m->vals, x, y, cal, ep, stream);
-        return dot ? launch_cfg<double, 16, kWPC, kStages, true>(m, m->vals, x, y, cal, ep, stream)
-                   : launch_cfg<double, 16, kWPC, kStages, false>(m, m->vals, x, y, cal, ep, stream);
+            return dot ? launch_idx<double, 16, kWPCL1, kStages, true>(m, m->vals, x, y, cal, ep, stream)
+                       : launch_idx<double, 16, kWPCL1, kStages, false>(m, m->vals, x, y, cal, ep, stream);
+        return dot ? launch_idx<double, 16, kWPC, kStages, true>(m, m->vals, x, y, cal, ep, stream)
+                   : launch_idx<double, 16, kWPC, kStages, false>(m, m->vals, x, y, cal, ep, stream);
     default:
         return fail(DIMGPU_ERR_UNSUPPORTED, "sigma %u has no SpMV kernel", m->sigma);
     }
@@ -475,10 +509,10 @@ int launch_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calib
     switch (m->sigma) {
     case 16:
         if (m->plan32.warps_per_cta == kWPC32L1)
-            return dot ? launch_cfg<float, 16, kWPC32L1, kStages, true>(m, m->vals32, x, y, cal, ep, stream)
-                       : launch_cfg<float, 16, kWPC32L1, kStages, false>(m, m->vals32, x, y, cal, ep, stream);
-        return dot ? launch_cfg<float, 16, kWPC32, kStages, true>(m, m->vals32, x, y, cal, ep, stream)
-                   : launch_cfg<float, 16, kWPC32, kStages, false>(m, m->vals32, x, y, cal, ep, stream);
+            return dot ? launch_idx<float, 16, kWPC32L1, kStages, true>(m, m->vals32, x, y, cal, ep, stream)
+                       : launch_idx<float, 16, kWPC32L1, kStages, false>(m, m->vals32, x, y, cal, ep, stream);
+        return dot ? launch_idx<float, 16, kWPC32, kStages, true>(m, m->vals32, x, y, cal, ep, stream)
+                   : launch_idx<float, 16, kWPC32, kStages, false>(m, m->vals32, x, y, cal, ep, stream);
     default:
         return fail(DIMGPU_ERR_UNSUPPORTED, "sigma %u has no SpMV kernel", m->sigma);
     }

@@ -25,12 +25,14 @@ struct word_of<32> {
     using type = uint64_t;
 };
 
-template <typename VT, int SIGMA>
+// One staged tile: its values, its column indices (u32, or u16 offsets from the tile's smallest column
+// when IDX16) and its 32 descriptor words.
+template <typename VT, int SIGMA, bool IDX16 = false>
 struct tile_geom {
     using Word = typename word_of<SIGMA>::type;
     static constexpr uint32_t TS = SIGMA * 32;
     static constexpr uint32_t VBYTES = TS * sizeof(VT);
-    static constexpr uint32_t CBYTES = TS * 4;
+    static constexpr uint32_t CBYTES = TS * (IDX16 ? 2 : 4);
     static constexpr uint32_t DBYTES = 32 * sizeof(Word);
     static constexpr uint32_t STAGE = VBYTES + CBYTES + DBYTES;
     static constexpr desc_fields F = fields_for(SIGMA, 32);
@@ -38,19 +40,32 @@ struct tile_geom {
     static constexpr uint64_t FMASK = (SIGMA == 64) ? ~0ull : ((1ull << SIGMA) - 1);
 };
 
-// Loads lane `lane`'s column (SIGMA values and column indices) from a shared stage.
-template <typename VT, int SIGMA>
-__device__ __forceinline__ void load_column(const unsigned char* stage, unsigned lane, VT (&v)[SIGMA],
-                                            uint32_t (&ci)[SIGMA]) {
-    using G = tile_geom<VT, SIGMA>;
-    const uint4* sc = reinterpret_cast<const uint4*>(stage + G::VBYTES);
+// Loads lane `lane`'s column (SIGMA values and column indices) from a shared stage; 16-bit indices are
+// offsets from `col_base`.
+template <typename VT, int SIGMA, bool IDX16 = false>
+__device__ __forceinline__ void load_column(const unsigned char* stage, unsigned lane, uint32_t col_base,
+                                            VT (&v)[SIGMA], uint32_t (&ci)[SIGMA]) {
+    using G = tile_geom<VT, SIGMA, IDX16>;
+    if constexpr (IDX16) {
+        const uint2* sc = reinterpret_cast<const uint2*>(stage + G::VBYTES);
 #pragma unroll
-    for (int j = 0; j < SIGMA / 4; ++j) {
-        const uint4 q = sc[j * 32 + lane];
-        ci[4 * j + 0] = q.x;
-        ci[4 * j + 1] = q.y;
-        ci[4 * j + 2] = q.z;
-        ci[4 * j + 3] = q.w;
+        for (int j = 0; j < SIGMA / 4; ++j) {
+            const uint2 q = sc[j * 32 + lane];  // four u16 in quad order
+            ci[4 * j + 0] = col_base + (q.x & 0xFFFFu);
+            ci[4 * j + 1] = col_base + (q.x >> 16);
+            ci[4 * j + 2] = col_base + (q.y & 0xFFFFu);
+            ci[4 * j + 3] = col_base + (q.y >> 16);
+        }
+    } else {
+        const uint4* sc = reinterpret_cast<const uint4*>(stage + G::VBYTES);
+#pragma unroll
+        for (int j = 0; j < SIGMA / 4; ++j) {
+            const uint4 q = sc[j * 32 + lane];
+            ci[4 * j + 0] = q.x;
+            ci[4 * j + 1] = q.y;
+            ci[4 * j + 2] = q.z;
+            ci[4 * j + 3] = q.w;
+        }
     }
     if constexpr (sizeof(VT) == 8) {
         const double2* sv = reinterpret_cast<const double2*>(stage);
@@ -125,10 +140,11 @@ __device__ __forceinline__ void chain_write_row(const tile_io<VT>& io, warp_chai
 // Processes tile t staged at `st` (its values, column indices and descriptor words).  raw / raw_next are
 // tile_ptr[t] and tile_ptr[t + 1] with their dirty bits.  The stage's value area is reused as the
 // staging buffer of the tile's closed rows; the caller must __syncwarp() before refilling the stage.
-template <typename VT, int SIGMA, bool DOT, int XM = kXReadOnly>
+template <typename VT, int SIGMA, bool DOT, int XM = kXReadOnly, bool IDX16 = false>
 __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned char* st, unsigned lane, uint64_t t,
-                                             uint32_t raw, uint32_t raw_next, uint64_t pol_keep, warp_chain<VT>& ch) {
-    using G = tile_geom<VT, SIGMA>;
+                                             uint32_t raw, uint32_t raw_next, uint64_t pol_keep, warp_chain<VT>& ch,
+                                             uint32_t col_base = 0) {
+    using G = tile_geom<VT, SIGMA, IDX16>;
     using Word = typename G::Word;
     const uint32_t row_stop = raw_next & ~kDirty;
     const uint32_t row_start = raw & ~kDirty;
@@ -136,7 +152,7 @@ __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned cha
 
     VT v[SIGMA];
     uint32_t ci[SIGMA];
-    load_column<VT, SIGMA>(st, lane, v, ci);
+    load_column<VT, SIGMA, IDX16>(st, lane, col_base, v, ci);
     const Word w = sd[lane];
     VT xv[SIGMA];
 #pragma unroll

@@ -190,7 +190,9 @@ def test_power_law_full_size(native, torch_cuda):
 
 
 def _launch_matrices(rng):
+    """Matrices whose tiles fit 16-bit column offsets, and one whose random columns do not (32-bit)."""
     yield random_csr(rng, 9000, 9000, 12.0, empty_frac=0.1, long_rows=4, long_len=(600, 6000))
+    yield random_csr(rng, 100000, 100000, 3.0, empty_frac=0.05, long_rows=3, long_len=(2000, 9000))
     yield csr_from_lengths([3] * 10000 + [20000] + [5] * 13999, 24000, rng)  # one row across many warp runs
     yield random_csr(rng, 3000, 3000, 2.0)
 
@@ -274,3 +276,21 @@ def test_launch_configuration_errors(native, torch_cuda):
     with pytest.raises(ValueError):
         A.set_spmv_launch(16, gather="texture")
     assert A.spmv_launch() == (16, "l1")  # small matrices keep the default
+
+
+def test_16_bit_column_offsets(native, torch_cuda):
+    """The converter keeps 16-bit column offsets exactly when every full tile's columns span less than
+    2^16 (device_bytes counts them), and the product is the oracle's either way."""
+    rng = np.random.default_rng(90)
+    narrow = random_csr(rng, 20000, 60000, 8.0)  # columns < 2^16: every tile fits
+    wide = random_csr(rng, 20000, 200000, 8.0)  # random columns over 200k: tiles span more
+    for m, has16 in ((narrow, True), (wide, False)):
+        A = csr5.from_csr(m)
+        T = A.tile_count
+        # everything but the offsets: values + indices, row_ptr, tile_ptr + tdo_ptr, descriptors (a few
+        # dirty tiles' tile_desc_offset entries stay far below the 2 bytes per element of the offsets)
+        base = 12 * m.nnz + 4 * (m.dimensions.rows + 1) + 8 * (T + 1) + 4 * T * 32
+        assert (A.device_bytes - base >= 2 * T * 512) == has16, (A.device_bytes - base, has16)
+        x = rng.uniform(-1, 1, m.dimensions.cols)
+        y_ref, ax = _refs(m, x)
+        assert_spmv_close(_gpu_spmv(torch_cuda, A, x), y_ref, ax, SPMV_RTOL_F64)
