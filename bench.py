@@ -402,7 +402,8 @@ def run_spmv_only(args):
     torch.cuda.synchronize()
     s = ev0.elapsed_time(ev1) * 1e-3 / args.steps
     nbytes = (8 * nnz + 8 * n) if args.f32 else (12 * nnz + 16 * n)
-    print(json.dumps({"spmv_seconds": s, "gbps": nbytes / s / 1e9, "nnz": nnz, "n": n, "f32": bool(args.f32)}))
+    print(json.dumps({"spmv_seconds": s, "gbps": nbytes / s / 1e9, "nnz": nnz, "n": n, "f32": bool(args.f32),
+                      "launch": A.spmv_launch(bool(args.f32))}))
     return 0
 
 
