@@ -19,8 +19,8 @@
 // reliable update flushes y into x and replaces r by the true f64 residual b - A x computed with the
 // f64 matrix.  Convergence is declared on a true f64 residual only.  Iteration kernels:
 //   A32 SpMV (f32) + s.As + alpha;  B32 r -= alpha As, y += alpha s, r.r, decides a reliable update;
-//   IF(reliable update) { x += y, y = 0;  Ax = A x (f64 SpMV);  r = b - Ax, r.r (f64) };
-//   S32 s = r + beta s.
+//   IF(reliable update) { x += y, y = 0;  Ax = A x (f64 SpMV);  r = b - Ax, r.r (f64);  S32 };
+//   beside the IF: S32 s = r + beta s (it returns at once when a reliable update is due).
 // The IF is a conditional graph node, so iterations without a reliable update launch three kernels.
 #include <cuda_runtime.h>
 
@@ -479,12 +479,14 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_ru_r_mixed(const double* b, 
     }
 }
 
-// s32 = r32 + beta s32 while the solve continues
+// s32 = r32 + beta s32 while the solve continues: after_ru = 0 runs it in iterations without a reliable
+// update (beside the reliable-update IF node in the graph, so that the node's evaluation is off the
+// iteration's critical path), after_ru = 1 after one (inside the IF body, from the replaced residual).
 __global__ void __launch_bounds__(kVecThreads, 2) k_update_s_mixed(float* s, const float* r, uint64_t n,
-                                                                const cg_state* st) {
-    const uint32_t stop = st->stop;
+                                                                const cg_state* st, int after_ru) {
+    const uint32_t stop = st->stop, no_ru = st->no_ru;
     const float beta = (float)st->beta;
-    if (stop)
+    if (stop || (after_ru ? no_ru != 0u : no_ru == 0u))
         return;
     const uint64_t pol = policy_evict_last();
     float4 sv[kUnroll], rv[kUnroll];
@@ -601,13 +603,15 @@ spmv_epilogue cg_epilogue(dimgpu_cg_solver* s) {
     return ep;
 }
 
-// The reliable-update kernels of the mixed solver (each guarded by st->no_ru).
+// The reliable-update kernels of the mixed solver, ending with the s update from the replaced residual
+// (each guarded by st->no_ru).
 int enqueue_reliable_update(dimgpu_cg_solver* s, const vec_ctx& c, cudaStream_t st) {
     k_flush_mixed<<<s->grid, kVecThreads, 0, st>>>(s->x, s->y32, s->n, s->st, 1);
     spmv_epilogue ru;
     ru.halt = &s->st->no_ru;
     DG_CHECK(launch_spmv_f64(s->m, s->x, s->Ax, &s->cal, ru, st));
     k_ru_r_mixed<<<s->grid, kVecThreads, 0, st>>>(s->b, s->Ax, s->r32, s->n, c);
+    k_update_s_mixed<<<s->grid, kVecThreads, 0, st>>>(s->s32, s->r32, s->n, s->st, 1);
     DG_CUDA(cudaGetLastError());
     return DIMGPU_OK;
 }
@@ -617,8 +621,8 @@ int enqueue_iteration(dimgpu_cg_solver* s, const vec_ctx& c, cudaStream_t st) {
     if (mixed(s)) {
         DG_CHECK(launch_spmv_f32(s->m, s->s32, s->As32, &s->cal, cg_epilogue(s), st));
         k_update_r_mixed<<<s->grid, kVecThreads, 0, st>>>(s->As32, s->r32, s->s32, s->y32, s->n, c);
+        k_update_s_mixed<<<s->grid, kVecThreads, 0, st>>>(s->s32, s->r32, s->n, s->st, 0);
         DG_CHECK(enqueue_reliable_update(s, c, st));
-        k_update_s_mixed<<<s->grid, kVecThreads, 0, st>>>(s->s32, s->r32, s->n, s->st);
     } else {
         DG_CHECK(launch_spmv_f64(s->m, s->s, s->As, &s->cal, cg_epilogue(s), st));
         k_update_r64<<<s->grid, kVecThreads, 0, st>>>(s->As, s->r, s->n, c);
@@ -673,7 +677,8 @@ int add_conditional(cudaGraph_t graph, const std::vector<cudaGraphNode_t>& deps,
 constexpr int kGraphUnroll = 4;
 
 // Graph: init kernels -> WHILE(loop) { kGraphUnroll iterations }.  A mixed iteration is
-// A32 -> B32 -> IF(ru) { flush, f64 SpMV, residual } -> S32, each IF with its own condition handle.
+// A32 -> B32 -> { IF(ru) { flush, f64 SpMV, residual, S32 after it }  ||  S32 (no reliable update) },
+// each IF with its own condition handle; the next iteration waits for both branches.
 int build_graph(dimgpu_cg_solver* s) {
     cudaGraph_t g = nullptr;
     DG_CUDA(cudaGraphCreate(&g, 0));
@@ -731,11 +736,15 @@ int build_graph(dimgpu_cg_solver* s) {
                 if ((rc = capture_into(cap, ibody, {}, nullptr,
                                        [&] { return enqueue_reliable_update(s, cu, cap); })) != DIMGPU_OK)
                     break;
-                rc = capture_into(cap, body, {inode}, &prev, [&]() -> int {
-                    k_update_s_mixed<<<s->grid, kVecThreads, 0, cap>>>(s->s32, s->r32, s->n, s->st);
+                // the s update of iterations without a reliable update, beside the IF node
+                std::vector<cudaGraphNode_t> sb;
+                rc = capture_into(cap, body, ab, &sb, [&]() -> int {
+                    k_update_s_mixed<<<s->grid, kVecThreads, 0, cap>>>(s->s32, s->r32, s->n, s->st, 0);
                     DG_CUDA(cudaGetLastError());
                     return DIMGPU_OK;
                 });
+                prev = sb;
+                prev.push_back(inode);
             }
             if (rc != DIMGPU_OK)
                 break;
