@@ -197,17 +197,39 @@ __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned cha
         VT sum = VT(0), red = VT(0);
         uint32_t k = 0;
         bool seen = false;
+        if (!__any_sync(kFull, (flag & (flag - 1u)) != 0u)) {
+            // No column holds two row starts (rows longer than sigma): no segment closes inside a column,
+            // so the loop keeps only the products and the restart at the row start.  Lane 0's head bit
+            // is applied afterwards; every sum is the same chain of fma as in the general loop.
 #pragma unroll
-        for (int r = 0; r < SIGMA; ++r) {
-            const bool bit = ((fl >> r) & 1u) != 0;
-            const bool close = bit && seen;
-            if (close)
-                slot[k] = sum;
-            k += close ? 1u : 0u;
-            red = (bit && !seen) ? sum : red;
-            seen = seen || bit;
-            sum = bit ? VT(0) : sum;
-            sum = fma(v[r], xv[r], sum);
+            for (int r = 0; r < SIGMA; ++r) {
+                const bool bit = ((flag >> r) & 1u) != 0;
+                red = bit ? sum : red;
+                sum = bit ? VT(0) : sum;
+                sum = fma(v[r], xv[r], sum);
+            }
+            seen = flag != 0u;
+            if (lane == 0) {
+                if ((flag >> 1) != 0u) {  // segment 0 closes at the column's row start
+                    slot[0] = red;
+                    k = 1;
+                }
+                red = VT(0);
+                seen = true;
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < SIGMA; ++r) {
+                const bool bit = ((fl >> r) & 1u) != 0;
+                const bool close = bit && seen;
+                if (close)
+                    slot[k] = sum;
+                k += close ? 1u : 0u;
+                red = (bit && !seen) ? sum : red;
+                seen = seen || bit;
+                sum = bit ? VT(0) : sum;
+                sum = fma(v[r], xv[r], sum);
+            }
         }
         const VT L = seen ? sum : VT(0);
         red = seen ? red : sum;
