@@ -86,14 +86,12 @@ __device__ bool grid_reduce_cols(double v1, double v2, uint32_t kp, const bctx& 
         c.part[(uint64_t)blockIdx.x * 64 + threadIdx.x] = a;
         c.part[(uint64_t)blockIdx.x * 64 + 32 + threadIdx.x] = b;
     }
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0)
-        s_last = (atomicAdd(c.counter, 1u) == gridDim.x - 1) ? 1u : 0u;
+        s_last = (ticket_acq_rel(c.counter) == gridDim.x - 1) ? 1u : 0u;
     __syncthreads();
     if (!s_last)
         return false;
-    __threadfence();
     if (threadIdx.x < kp) {
         double a = 0, b = 0;
         for (unsigned blk = 0; blk < gridDim.x; ++blk) {

@@ -69,13 +69,11 @@ __device__ bool grid_reduce2(double a, double b, const vec_ctx& c, double* ta, d
         }
         c.part[2 * blockIdx.x] = x;
         c.part[2 * blockIdx.x + 1] = y;
-        __threadfence();
-        s_last = (atomicAdd(c.counter, 1u) == gridDim.x - 1) ? 1u : 0u;
+        s_last = (ticket_acq_rel(c.counter) == gridDim.x - 1) ? 1u : 0u;
     }
     __syncthreads();
     if (!s_last)
         return false;
-    __threadfence();
     double x = 0, y = 0;
     for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
         x += __ldcg(&c.part[2 * i]);

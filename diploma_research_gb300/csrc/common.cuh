@@ -117,6 +117,16 @@ __device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Completion ticket: adds 1 to *p with acquire-release semantics at GPU scope and returns the old value.
+// Called by one thread after a __syncthreads(): the block's earlier writes are released with it, and
+// the block that draws the last ticket has acquired every earlier block's writes once it passes its next
+// __syncthreads() (no separate fences on either side).
+__device__ __forceinline__ uint32_t ticket_acq_rel(uint32_t* p) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+    return old;
+}
+
 // Bounded wait for run k's flag of this launch; returns its fragment kind, or kFragNone after recording
 // kStatusWaitTimeout.  Polls without acquire (no cache invalidation per poll), then one acquire.
 __device__ __forceinline__ uint32_t wait_run(const uint32_t* flag, uint32_t epoch, uint32_t* status) {

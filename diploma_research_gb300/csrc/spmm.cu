@@ -557,14 +557,11 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        s_last = (atomicAdd(&p.words[0], 1u) == gridDim.x - 1) ? 1u : 0u;
-    }
+    if (threadIdx.x == 0)
+        s_last = (ticket_acq_rel(&p.words[0]) == gridDim.x - 1) ? 1u : 0u;
     __syncthreads();
     if (!s_last)
         return;
-    __threadfence();
 
     double fix_dot = 0.0;
     const uint64_t first_tail = p.T * kTS;

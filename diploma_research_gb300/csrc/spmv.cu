@@ -256,14 +256,12 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
                 d += s_red[w];
             p.cta_part[cta] = d;
         }
-        __threadfence();
-        const uint32_t ticket = atomicAdd(&p.words[0], 1u);
+        const uint32_t ticket = ticket_acq_rel(&p.words[0]);
         s_last = (ticket == gridDim.x - 1) ? 1u : 0u;
     }
     __syncthreads();
     if (!s_last)
         return;
-    __threadfence();
 
     // CSR tail (csr5.h:756-782): one row per thread; a first row that began inside the tiles is closed
     // by looking back over the runs like any other row.
