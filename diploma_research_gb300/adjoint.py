@@ -1,4 +1,4 @@
-"""Differentiation through x = A^{-1} b (the spec adjoint variant; the reference has none).
+"""Differentiation through x = A^{-1} b (the adjoint variant of the solver; the reference has none).
 
 For a loss L(x) with g = dL/dx:  lambda = A^{-T} g,  dL/db = lambda,  dL/dA = -lambda x^T on the pattern.
 All arrays are device arrays (``__cuda_array_interface__``, float64); gradients of A come in the CSR

@@ -8,7 +8,7 @@
 // A^T is built once per matrix, deterministically: the device arrays are put back in CSR order on the
 // device, the transpose is a stable counting sort on the host (rows of A^T keep increasing column
 // order), and the result goes through the normal device CSR5 conversion, so A^T x runs on the same
-// SpMV kernel as A x.  The reference has no adjoint; this is the spec differentiation variant.
+// SpMV kernel as A x.  The reference has no adjoint; this is the differentiation variant of its solver.
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -632,7 +632,7 @@ int check_status(dimgpu_calibrator* cal, cudaStream_t stream) {
 // partials, the completion ticket and the status word), and dimgpu_calibrator_create obtains it
 // with cudaMalloc.  Some callers cannot do that: a plugin running inside a host application that
 // reserved all device memory up front, a real-time loop where cudaMalloc's implicit device
-// synchronisation would break the latency budget, or code that must not grow its memory footprint
+// synchronisation would break its latency bound, or code that must not grow its memory footprint
 // after start-up.  For them the scratch of this entry point is a fixed array compiled into the
 // library: every GPU that loads the library holds it until the process exits.
 // ------------------------------------------------------------------------------------------------

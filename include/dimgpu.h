@@ -148,7 +148,7 @@ DIMGPU_API int dimgpu_csr5_spmv_static_scratch(const dimgpu_csr5* m, const doubl
 
 /* ---- several right-hand sides ------------------------------------------------------------------- */
 
-/* Y := A X for k right-hand sides (the spec batching of csr5::spmv): X is cols x k, Y rows x k,
+/* Y := A X for k right-hand sides (the batched form of csr5::spmv): X is cols x k, Y rows x k,
  * both row-major with leading dimensions ldx, ldy >= k (device memory).  k > 32 runs in passes of 32
  * columns.  The first call for a given (k, precision) times the candidate launch shapes on these
  * operands and keeps the fastest (make it outside any stream capture).  Calls on one matrix must not

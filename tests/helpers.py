@@ -32,7 +32,7 @@ def csr_from_lengths(lens, cols, rng):
 
 
 # Componentwise SpMV tolerance: |y - y_ref|_i <= RTOL * (|A| |x|)_i (+ a tiny absolute floor for
-# rows whose |A||x| is 0).  FP64 parity bar of the benchmark spec: 1e-12.
+# rows whose |A||x| is 0).  FP64 parity bar: 1e-12.
 SPMV_RTOL_F64 = 1e-12
 SPMV_RTOL_F32 = 2e-6
 
