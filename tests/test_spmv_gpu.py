@@ -86,6 +86,38 @@ def test_edge_cases(native, torch_cuda, lens, cols):
     _check(torch_cuda, m, rng.uniform(-1, 1, cols))
 
 
+def _single_start_matrices(rng):
+    """Matrices whose tiles take the single-row-start segment loop (no 16-element column holds two row
+    starts), with the cases that loop treats apart: a row start at every position of a column, columns
+    without one, lane 0 with and without a row start at r = 0, empty rows (several rows starting at one
+    element, dirty tiles), and one short row that sends its tile down the general loop."""
+    yield csr_from_lengths(rng.integers(16, 48, 4000), 5000, rng)
+    yield csr_from_lengths([16] * 3000, 3000, rng)  # every column begins a row at r = 0
+    yield csr_from_lengths([17] * 3000, 3000, rng)  # the row start walks through every r
+    lens = rng.integers(16, 40, 3000)
+    lens[rng.choice(3000, 300, replace=False)] = 0
+    yield csr_from_lengths(lens, 4000, rng)
+    lens = rng.integers(16, 40, 3000)
+    lens[1500] = 3
+    yield csr_from_lengths(lens, 4000, rng)
+
+
+def test_single_row_start_columns(native, torch_cuda):
+    """The segment loop for tiles whose columns hold at most one row start, in f64 and f32, against the
+    oracle."""
+    torch = torch_cuda
+    rng = np.random.default_rng(91)
+    for m in _single_start_matrices(rng):
+        x = rng.uniform(-1, 1, m.dimensions.cols)
+        A, _ = _check(torch, m, x)
+        xd = torch.tensor(x, device="cuda", dtype=torch.float32)
+        yd = torch.full((m.dimensions.rows,), float("nan"), device="cuda", dtype=torch.float32)
+        A.spmv(xd, yd)
+        torch.cuda.synchronize()
+        y_ref, ax = _refs(m, x.astype(np.float32).astype(np.float64))
+        assert_spmv_close(yd.cpu().numpy().astype(np.float64), y_ref, ax, SPMV_RTOL_F32 * 50)
+
+
 def test_many_warps_share_a_row(native, torch_cuda):
     """A row long enough to cover several warps' tile runs exercises chained calibrator slots."""
     rng = np.random.default_rng(77)
