@@ -148,13 +148,22 @@ def _workload():
     return m, xs, b
 
 
+def _config(m):
+    """The workload description both arms print (identical strings for one and the same system)."""
+    n, nnz = m.dimensions.rows, m.nnz
+    mb = (12 * nnz + 4 * (n + 1)) / 1e6
+    return {"workload": f"{WORKLOAD}: {DESCR[WORKLOAD]}, n={n}, nnz={nnz}, CG to {TOL:g} from x0 = 0, FP64",
+            "global_batch": 1, "seq_len": n,
+            "l2": f"{mb:.0f} MB of CSR data vs 129 MB L2" + ("; no flush" if mb > 135 else
+                                                             "; L2-resident, no flush (solve-level timing)")}
+
+
 def run_reference(args):
-    """The reference's CPU CG (oracle/csr5_oracle.c restating csr5.h + dim_sp) on all host threads."""
+    """The reference's CPU CG (oracle/csr5_oracle.c restating csr5.h + dim_sp) on all host threads: one
+    full solve to the tolerance per step."""
     ws, rank, _ = _dist()
     if rank != 0:
         return 0
-    import numpy as np
-
     import oracle
 
     m, xs, b = _workload()
@@ -163,25 +172,20 @@ def run_reference(args):
     t0 = time.perf_counter()
     o = oracle.OracleCSR5(n, n, m.row_start_offsets, m.col_indices, m.values, 16, 4)
     convert_s = time.perf_counter() - t0
-    # iterations to converge: one full solve, untimed
-    _, iters, rel = o.cg(b, tol=TOL, nthreads=threads)
-    sample_it = min(iters, 25)
     for _ in range(args.warmup):
-        o.cg(b, tol=TOL, max_it=sample_it, nthreads=threads)
+        _, iters, rel = o.cg(b, tol=TOL, nthreads=threads)
     times = []
     for _ in range(args.steps):
         t = time.perf_counter()
-        o.cg(b, tol=TOL, max_it=sample_it, nthreads=threads)
+        _, iters, rel = o.cg(b, tol=TOL, nthreads=threads)
         times.append(time.perf_counter() - t)
-    per_it = statistics.mean(times) / sample_it
-    value = per_it * iters
-    sample = (f"{sample_it} CG iterations per step on the full {WORKLOAD} system, scaled to the {iters} iterations "
-              f"the same CPU CG needs to reach {TOL:g} (one full untimed solve, rel. residual {rel:.2e})")
+    value = statistics.mean(times)
+    sample = (f"full CPU CG solves of {WORKLOAD} to {TOL:g} ({iters} iterations, rel. residual {rel:.2e}), "
+              f"one per step, oracle/csr5_oracle.c on {threads} host threads")
     out = {"metric": METRIC, "value": value, "unit": "s", "impl": "reference", "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(times) * 1e3,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": f"{WORKLOAD}: {DESCR[WORKLOAD]}, n={n}, nnz={m.nnz}, CG to {TOL:g}",
-                      "global_batch": 1, "parallelism": "cpu-openmp"},
+           "config": _config(m), "execution": f"CPU, OpenMP on {threads} threads",
            "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "iterations": iters, "convert_s": convert_s}
@@ -238,7 +242,8 @@ def run_gpu(args):
     torch.cuda.synchronize()
     sec64 = ev0.elapsed_time(ev1) * 1e-3 / args.steps
     sec64 = _barrier_max(sec64, ws)
-    err64 = float(np.linalg.norm(xd.cpu().numpy() - xs) / np.linalg.norm(xs))
+    x64 = xd.cpu().numpy()
+    err64 = float(np.linalg.norm(x64 - xs) / np.linalg.norm(xs))
     res64 = r
 
     # ---- mixed-precision CG ----
@@ -251,7 +256,8 @@ def run_gpu(args):
     ev1.record(stream)
     torch.cuda.synchronize()
     secm = _barrier_max(ev0.elapsed_time(ev1) * 1e-3 / args.steps, ws)
-    errm = float(np.linalg.norm(xd.cpu().numpy() - xs) / np.linalg.norm(xs))
+    xmx = xd.cpu().numpy()
+    errm = float(np.linalg.norm(xmx - xs) / np.linalg.norm(xs))
 
     # ---- FP64 SpMV alone: the dominant kernel, for the roofline ----
     x1 = torch.tensor(np.random.default_rng(5).uniform(-1, 1, n), device="cuda", dtype=torch.float64)
@@ -325,17 +331,21 @@ def run_gpu(args):
 
     # ---- CPU baseline: the reference's CPU CG (C restatement), full solve, rank 0 only ----
     cpu = None
+    oracle_err = {"fp64": None, "mixed": None, "oracle_iterations": None}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         import oracle
 
         o = oracle.OracleCSR5(n, n, m.row_start_offsets, m.col_indices, m.values, 16, 4)
         threads = os.cpu_count() or 1
         t = time.perf_counter()
-        _, it_cpu, _ = o.cg(b, tol=TOL, nthreads=threads)
+        x_oracle, it_cpu, _ = o.cg(b, tol=TOL, nthreads=threads)
         cpu_s = time.perf_counter() - t
         cpu = {"value": cpu_s, "unit": "s", "cores": threads, "kind": "port",
                "sample": f"one full CPU CG solve of {WORKLOAD} to {TOL:g} ({it_cpu} iterations), "
                          f"oracle/csr5_oracle.c on {threads} host threads"}
+        xo_norm = float(np.linalg.norm(x_oracle))
+        oracle_err = {"fp64": float(np.linalg.norm(x64 - x_oracle) / xo_norm),
+                      "mixed": float(np.linalg.norm(xmx - x_oracle) / xo_norm), "oracle_iterations": it_cpu}
 
     launches_per_solve = 4 + 3 * statistics.mean(iters64)  # init SpMV + init, 3 per iteration, final SpMV + norms
     clocks = clk.summary()
@@ -344,15 +354,15 @@ def run_gpu(args):
             "metric": METRIC, "value": sec64, "unit": "s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": sec64 * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": f"synthetic (seeded {WORKLOAD}, b = A x*, x* ~ U[-1,1])",
-            "config": {"workload": f"{WORKLOAD}: {DESCR[WORKLOAD]}, n={n}, nnz={nnz}, CG to {TOL:g} "
-                                   "from x0 = 0, FP64", "global_batch": 1, "seq_len": n,
-                       "parallelism": "replicas" if ws > 1 else "single-gpu",
-                       "l2": f"inputs of {A.device_bytes / 1e6:.0f} MB of CSR5 data vs 129 MB L2"
-                             + ("; no flush" if A.device_bytes > 135e6 else "; L2-resident, no flush (solve-level timing)")},
+            "config": _config(m),
+            "execution": (f"{ws} replicas, one GPU each" if ws > 1 else "one GPU")
+                         + f", {A.device_bytes / 1e6:.0f} MB of CSR5 data on the device",
             "iterations": res64.iterations, "rel_residual": res64.rel_residual, "rel_error_vs_xstar": err64,
+            "rel_error_vs_oracle": oracle_err["fp64"], "oracle_iterations": oracle_err["oracle_iterations"],
             "mixed": {"value": secm, "unit": "s", "iterations": resm.iterations,
                       "reliable_updates": resm.reliable_updates, "rel_residual": resm.rel_residual,
-                      "rel_error_vs_xstar": errm, "speedup_vs_fp64": sec64 / secm, "dtype": "f32 inner / f64"},
+                      "rel_error_vs_xstar": errm, "rel_error_vs_oracle": oracle_err["mixed"],
+                      "speedup_vs_fp64": sec64 / secm, "dtype": "f32 inner / f64"},
             "spmv": {"seconds": spmv_s, "gbps": spmv_gbs, "bytes_per_launch": spmv_bytes,
                      "fp64_tflops": 2 * nnz / spmv_s / 1e12, "dot_fused_seconds": spmv_dot_s,
                      "f32_seconds": spmv32_s, "f32_gbps": (8 * nnz + 8 * n) / spmv32_s / 1e9},

@@ -29,8 +29,11 @@ MEM_DEVICE = 1
 CG_FP64 = 0
 CG_MIXED = 1
 
+TEST_LIB_PATH = os.path.join(HERE, "_lib", "libdimgpu_test.so")
+
 _lock = threading.Lock()
 _lib = None
+_test_lib = None
 
 
 class csr5_options(ctypes.Structure):
@@ -123,6 +126,9 @@ _SIGNATURES = {
     "dimgpu_csr5_spmv_transpose": [_vp, _vp, _vp, _vp],
     "dimgpu_csr5_pattern_outer": [_vp, _vp, _vp, _f64, _vp, _vp],
     "dimgpu_cg_adjoint": [_vp, _vp, _vp, _vp, _vp, ctypes.POINTER(cg_params), ctypes.POINTER(cg_stats), _vp],
+    "dimgpu_csr5_status": [_vp, _vp, _vp],
+    "dimgpu_static_scratch_status": [_vp],
+    "dimgpu_csr5_spmv_static_scratch": [_vp, _vp, _vp, _vp],
     "dimgpu_version": [],
 }
 
@@ -136,6 +142,17 @@ def declared_symbols():
         return re.findall(r"DIMGPU_API\s+(?:const\s+)?\w+\*?\s+\*?(dimgpu_\w+)\(", fh.read())
 
 
+def _load(path):
+    L = ctypes.CDLL(path)
+    for name, args in _SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    L.dimgpu_last_error_string.argtypes = []
+    L.dimgpu_last_error_string.restype = ctypes.c_char_p
+    return L
+
+
 def lib():
     """The loaded library; raises when it is missing (there is no CPU fallback)."""
     global _lib
@@ -143,15 +160,25 @@ def lib():
         if _lib is None:
             if not os.path.isfile(LIB_PATH):
                 raise ImportError(f"{LIB_PATH} is missing: build it with diploma_research_gb300.build.build()")
-            L = ctypes.CDLL(LIB_PATH)
-            for name, args in _SIGNATURES.items():
-                fn = getattr(L, name)
-                fn.argtypes = args
-                fn.restype = ctypes.c_int
-            L.dimgpu_last_error_string.argtypes = []
-            L.dimgpu_last_error_string.restype = ctypes.c_char_p
-            _lib = L
+            _lib = _load(LIB_PATH)
     return _lib
+
+
+def test_lib():
+    """libdimgpu_test.so: the same library built with test hooks and 20 ms device waits.  Only the
+    tests of the device status words load it; its handles must not be passed to lib()'s functions."""
+    global _test_lib
+    with _lock:
+        if _test_lib is None:
+            if not os.path.isfile(TEST_LIB_PATH):
+                raise ImportError(f"{TEST_LIB_PATH} is missing: build it with build(variant='test')")
+            L = _load(TEST_LIB_PATH)
+            L.dimgpu_test_withhold_run.argtypes = [_u32]
+            L.dimgpu_test_withhold_run.restype = None
+            L.dimgpu_test_set_spmv_grid.argtypes = [_vp, ctypes.c_int]
+            L.dimgpu_test_set_spmv_grid.restype = ctypes.c_int
+            _test_lib = L
+    return _test_lib
 
 
 def check(rc: int) -> int:

@@ -2,6 +2,11 @@
 
 One nvcc process per translation unit, run in parallel, then one link step.  The library links the
 CUDA runtime statically and depends on nothing from PyTorch.
+
+``build(variant="test")`` builds a second library, libdimgpu_test.so, from the same sources with
+DIMGPU_TEST_HOOKS defined and a 20 ms limit on every bounded device wait (DIMGPU_WAIT_NS): it adds
+hooks that make a wait run out on purpose, for the tests of the device status words.  The product
+never loads it.
 """
 from __future__ import annotations
 
@@ -17,6 +22,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 BUILD_DIR = os.path.join(ROOT, "_build", "dimgpu")
 LIB = os.path.join(OUT_DIR, "libdimgpu.so")
+TEST_LIB = os.path.join(OUT_DIR, "libdimgpu_test.so")
+TEST_FLAGS = ["-DDIMGPU_TEST_HOOKS", "-DDIMGPU_WAIT_NS=20000000ull"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "-fPIC",
@@ -46,36 +53,51 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
-def build(verbose: bool = False, force: bool = False, extra_flags=()) -> str:
-    os.makedirs(OUT_DIR, exist_ok=True)
-    os.makedirs(BUILD_DIR, exist_ok=True)
+def _run(cmd, verbose):
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if verbose and (r.stdout or r.stderr):
+        print(r.stdout, r.stderr, file=sys.stderr)
+
+
+def build(verbose: bool = False, force: bool = False, extra_flags=(), variant: str = "product") -> str:
+    """Builds one variant ("product": libdimgpu.so, "test": libdimgpu_test.so); returns its path."""
+    return build_variants((variant,), verbose=verbose, force=force, extra_flags=extra_flags)[0]
+
+
+def build_variants(variants=("product", "test"), verbose: bool = False, force: bool = False, extra_flags=()):
+    """Builds the given variants, all translation units of all of them in one parallel pool."""
     nv = nvcc()
     hdrs = headers()
-    objs, jobs = [], []
-    for src in sources():
-        obj = os.path.join(BUILD_DIR, os.path.basename(src)[:-3] + ".o")
-        objs.append(obj)
-        if force or _stale(obj, [src] + hdrs):
-            cmd = [nv, *ARCH, *NVCC_FLAGS, *extra_flags, "-c", src, "-o", obj]
-            jobs.append(cmd)
-
-    def run(cmd):
-        if verbose:
-            print(" ".join(cmd), flush=True)
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"nvcc failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
-        if verbose and (r.stdout or r.stderr):
-            print(r.stdout, r.stderr, file=sys.stderr)
-
+    os.makedirs(OUT_DIR, exist_ok=True)
+    jobs, links = [], []
+    for variant in variants:
+        if variant not in ("product", "test"):
+            raise ValueError(f"unknown variant {variant!r}")
+        lib_path = TEST_LIB if variant == "test" else LIB
+        build_dir = BUILD_DIR + ("_test" if variant == "test" else "")
+        flags = list(extra_flags) + (TEST_FLAGS if variant == "test" else [])
+        os.makedirs(build_dir, exist_ok=True)
+        objs, fresh = [], False
+        for src in sources():
+            obj = os.path.join(build_dir, os.path.basename(src)[:-3] + ".o")
+            objs.append(obj)
+            if force or _stale(obj, [src] + hdrs):
+                jobs.append([nv, *ARCH, *NVCC_FLAGS, *flags, "-c", src, "-o", obj])
+                fresh = True
+        links.append((lib_path, objs, fresh))
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
-            list(ex.map(run, jobs))
-    if force or jobs or _stale(LIB, objs):
-        run([nv, *ARCH, "-shared", "-o", LIB, *objs])
-    return LIB
+            list(ex.map(lambda c: _run(c, verbose), jobs))
+    for lib_path, objs, fresh in links:
+        if force or fresh or _stale(lib_path, objs):
+            _run([nv, *ARCH, "-shared", "-o", lib_path, *objs], verbose)
+    return [lp for lp, _, _ in links]
 
 
 if __name__ == "__main__":
-    build(verbose="-v" in sys.argv, force="-f" in sys.argv)
-    print(LIB)
+    print(build(verbose="-v" in sys.argv, force="-f" in sys.argv,
+                variant="test" if "--test" in sys.argv else "product"))

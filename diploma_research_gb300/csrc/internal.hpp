@@ -130,6 +130,10 @@ int launch_spmv_f64(const dimgpu_csr5* m, const double* x, double* y, dimgpu_cal
 int launch_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calibrator* cal,
                     const spmv_epilogue& ep, cudaStream_t stream);
 int check_status(dimgpu_calibrator* cal, cudaStream_t stream);
+// Copies a device status word to *out (after synchronizing `stream`) and clears it when it is set.
+int take_status_word(uint32_t* word, cudaStream_t stream, uint32_t* out);
+// DIMGPU_OK for kStatusOk, else the matching DIMGPU_ERR_* with a message naming `where`.
+int status_error(uint32_t st, const char* where);
 int autotune_gathers(dimgpu_csr5* m, cudaStream_t stream);
 int autotune_f32(dimgpu_csr5* m, cudaStream_t stream);
 int vec_fill(uint64_t n, double v, double* y, cudaStream_t stream);

@@ -35,11 +35,12 @@
 // CSR tail (csr5.h:756-782) and, optionally, the fused dot x.y (per-CTA partials, fixed order) and
 // alpha = rr / (x.y) for CG.  y is fully overwritten: empty rows below the tail are zeroed from the
 // list built at conversion.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <vector>
 #include <mutex>
+#include <vector>
 
 #include "common.cuh"
 #include "internal.hpp"
@@ -48,6 +49,12 @@
 
 namespace dimgpu {
 namespace {
+
+#ifdef DIMGPU_TEST_HOOKS
+// Test builds only (libdimgpu_test.so): the warp run whose look-back flag the next launches withhold, so
+// that a later run's bounded look-back wait expires and the status query reports it.
+uint32_t g_test_withhold_run = 0xffffffffu;
+#endif
 
 template <typename VT>
 struct spmv_params {
@@ -80,6 +87,9 @@ struct spmv_params {
     const double* rr;
     double* alpha_out;
     uint32_t* halt;
+#ifdef DIMGPU_TEST_HOOKS
+    uint32_t withhold_run;  // test builds only: this run never publishes its flag word (0xffffffff = none)
+#endif
 };
 
 // Final value of row R, whose last fragment `own` this caller holds: the runs before `run` that hold
@@ -230,7 +240,10 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
                 p.frag_row[run] = ch.cal_row;
                 kind = kFragThrough;
             }
-            st_release_u32(&p.flag[run], (epoch << 2) | kind);
+#ifdef DIMGPU_TEST_HOOKS
+            if (run != p.withhold_run)
+#endif
+                st_release_u32(&p.flag[run], (epoch << 2) | kind);
             // rows this run finishes: its open row when it ends here, and the row it began inside
             if (ch.open && !cont_after)
                 chain_write_row<VT, DOT>(io, ch, 0, ch.carry_row, ch.carry);
@@ -360,6 +373,9 @@ int launch_cfg(const dimgpu_csr5* m, const VT* vals, const VT* x, VT* y, dimgpu_
     p.rr = ep.rr;
     p.alpha_out = ep.alpha_out;
     p.halt = ep.halt;
+#ifdef DIMGPU_TEST_HOOKS
+    p.withhold_run = g_test_withhold_run;
+#endif
     if ((sizeof(VT) == 8 ? m->x_mode : m->x_mode32) == kXStream)
         k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXStream, IDX16><<<pl.grid, WPC * 32, smem, stream>>>(p);
     else
@@ -609,18 +625,33 @@ int autotune_f32(dimgpu_csr5* m, cudaStream_t stream) {
     return rc;
 }
 
-int check_status(dimgpu_calibrator* cal, cudaStream_t stream) {
-    uint32_t st = 0;
-    DG_CUDA(cudaMemcpyAsync(&st, cal->status, sizeof(st), cudaMemcpyDeviceToHost, stream));
+int take_status_word(uint32_t* word, cudaStream_t stream, uint32_t* out) {
+    *out = kStatusOk;
+    if (!word)
+        return DIMGPU_OK;
+    DG_CUDA(cudaMemcpyAsync(out, word, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
     DG_CUDA(cudaStreamSynchronize(stream));
+    if (*out != kStatusOk)
+        DG_CUDA(cudaMemsetAsync(word, 0, sizeof(uint32_t), stream));
+    return DIMGPU_OK;
+}
+
+int status_error(uint32_t st, const char* where) {
     if (st == kStatusOk)
         return DIMGPU_OK;
-    cudaMemsetAsync(cal->status, 0, sizeof(uint32_t), stream);
     if (st == kStatusWaitTimeout)
-        return fail(DIMGPU_ERR_TIMEOUT, "a bounded device wait expired");
+        return fail(DIMGPU_ERR_TIMEOUT, "%s: a bounded device wait expired (the results of that launch are invalid)",
+                    where);
     if (st == kStatusBreakdown)
-        return fail(DIMGPU_ERR_BREAKDOWN, "CG breakdown: s.As <= 0 or not finite");
-    return fail(DIMGPU_ERR_BAD_INDEX, "device status %u", st);
+        return fail(DIMGPU_ERR_BREAKDOWN, "%s: CG breakdown: s.As <= 0 or not finite", where);
+    return fail(DIMGPU_ERR_BAD_INDEX, "%s: a device-side consistency check on the CSR5 arrays failed (status %u)",
+                where, st);
+}
+
+int check_status(dimgpu_calibrator* cal, cudaStream_t stream) {
+    uint32_t st = 0;
+    DG_CHECK(take_status_word(cal->status, stream, &st));
+    return status_error(st, "SpMV");
 }
 
 }  // namespace dimgpu
@@ -644,31 +675,100 @@ constexpr size_t kStaticValBytes = 8 * kStaticSlots;
 constexpr size_t kStaticDotBytes = 8 * (kStaticSlots + 32);
 constexpr size_t kStaticRowBytes = 4 * kStaticSlots;
 constexpr size_t kStaticFlagBytes = 4 * kStaticSlots;
-constexpr size_t kStaticWordBytes = 256;  // ticket, status, run counter, epoch: own 256-byte block
+// ticket, -, run counter, epoch (the kernel's control words), then the status word: own 256-byte block
+constexpr size_t kStaticWordBytes = 256;
 constexpr size_t kStaticScratchBytes =
     kStaticValBytes + kStaticDotBytes + kStaticRowBytes + kStaticFlagBytes + kStaticWordBytes;
+constexpr size_t kStaticWordsOffset = kStaticValBytes + kStaticDotBytes + kStaticRowBytes + kStaticFlagBytes;
+constexpr int kStaticStatusWord = 4;  // index of the status word in the control block
 
 // 98,816 bytes of device memory, shared by every call of dimgpu_csr5_spmv_static_scratch on a device.
 static __device__ __align__(256) unsigned char g_spmv_static_scratch[kStaticScratchBytes];
 
+// The array's device address is looked up once per device and context and cached.  A context is named by
+// its driver-assigned id (cuCtxGetId, unique for the life of the process), so a cached address is never
+// used in a context other than the one it was looked up in -- after cudaDeviceReset the primary context
+// is a new one, the module is loaded again and the address looked up again.
 constexpr int kMaxDevices = 64;
+struct static_slot {
+    bool valid = false;
+    unsigned long long ctx_id = 0;
+    unsigned char* addr = nullptr;
+};
 std::mutex g_static_mu;
-unsigned char* g_static_addr[kMaxDevices] = {};
+static_slot g_static[kMaxDevices];
+
+using pfn_ctx_get_current = CUresult (*)(CUcontext*);
+using pfn_ctx_get_id = CUresult (*)(CUcontext, unsigned long long*);
+
+// Id of the calling thread's current context; false when there is none or the driver cannot say.
+bool current_context_id(unsigned long long* id) {
+    static std::once_flag once;
+    static pfn_ctx_get_current get_current = nullptr;
+    static pfn_ctx_get_id get_id = nullptr;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void* f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<pfn_ctx_get_current>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<pfn_ctx_get_id>(f);
+        (void)cudaGetLastError();
+    });
+    if (!get_current || !get_id)
+        return false;
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx)
+        return false;
+    return get_id(ctx, id) == CUDA_SUCCESS;
+}
 
 // Device address of the static scratch on `device` (which must be current).  Host code cannot use
 // the symbol itself: on the host, g_spmv_static_scratch is only a stand-in, not a device address.
 int static_scratch_on(int device, unsigned char** out) {
     if (device < 0 || device >= kMaxDevices)
         return fail(DIMGPU_ERR_UNSUPPORTED, "device ordinal %d is beyond %d", device, kMaxDevices);
+    unsigned long long id = 0;
+    bool have_id = current_context_id(&id);
     std::lock_guard<std::mutex> lock(g_static_mu);
-    if (!g_static_addr[device]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_spmv_static_scratch);
-        if (e != cudaSuccess)
-            return cuda_fail(e, "cudaGetSymbolAddress(static SpMV scratch)");
-        g_static_addr[device] = static_cast<unsigned char*>(p);
+    static_slot& slot = g_static[device];
+    if (have_id && slot.valid && slot.ctx_id == id) {
+        *out = slot.addr;
+        return DIMGPU_OK;
     }
-    *out = g_static_addr[device];
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_spmv_static_scratch);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaGetSymbolAddress(static SpMV scratch)");
+    if (!have_id)
+        have_id = current_context_id(&id);  // the lookup made the primary context current
+    slot.valid = have_id;
+    slot.ctx_id = id;
+    slot.addr = static_cast<unsigned char*>(p);
+    *out = slot.addr;
+    return DIMGPU_OK;
+}
+
+// The static scratch of the current device, laid out as a calibrator.
+int static_calibrator(const dimgpu_csr5* m, dimgpu_calibrator* cal) {
+    int device = -1;
+    DG_CUDA(cudaGetDevice(&device));
+    if (m && device != m->device)
+        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "the matrix lives on device %d, the current device is %d",
+                    m->device, device);
+    unsigned char* base = nullptr;
+    DG_CHECK(static_scratch_on(device, &base));
+    cal->device = device;
+    cal->nslots = kStaticSlots;
+    cal->cal_val = reinterpret_cast<double*>(base);
+    cal->dot_part = reinterpret_cast<double*>(base + kStaticValBytes);
+    cal->cal_row = reinterpret_cast<uint32_t*>(base + kStaticValBytes + kStaticDotBytes);
+    cal->flag = reinterpret_cast<uint32_t*>(base + kStaticValBytes + kStaticDotBytes + kStaticRowBytes);
+    cal->counter = reinterpret_cast<uint32_t*>(base + kStaticWordsOffset);
+    cal->status = cal->counter + kStaticStatusWord;
     return DIMGPU_OK;
 }
 
@@ -716,32 +816,74 @@ extern "C" int dimgpu_csr5_spmv_static_scratch(const dimgpu_csr5* m, const doubl
     using namespace dimgpu;
     if (!m || (!x && m->cols) || (!y && m->rows))
         return fail(DIMGPU_ERR_INVALID_ARGUMENT, "NULL argument");
-    int device = -1;
-    DG_CUDA(cudaGetDevice(&device));
-    if (device != m->device)
-        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "the matrix lives on device %d, the current device is %d",
-                    m->device, device);
     if (m->plan.nwarps > kStaticSlots)
         return fail(DIMGPU_ERR_INVALID_ARGUMENT,
                     "this matrix's SpMV uses %u warp slots; the static scratch holds at most %u "
                     "(use dimgpu_csr5_spmv with a calibrator)",
                     m->plan.nwarps, kStaticSlots);
-    unsigned char* base = nullptr;
-    DG_CHECK(static_scratch_on(device, &base));
     dimgpu_calibrator cal;
-    cal.device = device;
-    cal.nslots = kStaticSlots;
-    cal.cal_val = reinterpret_cast<double*>(base);
-    cal.dot_part = reinterpret_cast<double*>(base + kStaticValBytes);
-    cal.cal_row = reinterpret_cast<uint32_t*>(base + kStaticValBytes + kStaticDotBytes);
-    cal.flag = reinterpret_cast<uint32_t*>(base + kStaticValBytes + kStaticDotBytes + kStaticRowBytes);
-    cal.counter = reinterpret_cast<uint32_t*>(base + kStaticValBytes + kStaticDotBytes + kStaticRowBytes +
-                                              kStaticFlagBytes);
-    cal.status = cal.counter + 1;
+    DG_CHECK(static_calibrator(m, &cal));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    // The array keeps whatever the previous call left; the completion ticket, the status word and the run
-    // counter must start at zero.  The launch epoch (word 3) carries over: the flags of earlier calls
-    // hold older epochs, and a zero-initialised array starts at epoch 0, which no launch uses.
+    // The array keeps whatever the previous call left.  The completion ticket and the run counter
+    // (control words 0-2) must start at zero; every launch leaves them so, but a launch that never ran to
+    // its end would not.  The launch epoch (word 3) carries over: the flags of earlier calls hold older
+    // epochs, and a zero-initialised array starts at epoch 0, which no launch uses.  The status word is
+    // left alone: a failure a kernel recorded stays there until dimgpu_static_scratch_status reads it.
     DG_CUDA(cudaMemsetAsync(cal.counter, 0, 3 * sizeof(uint32_t), s));
     return launch_spmv_f64(m, x, y, &cal, spmv_epilogue{}, s);
 }
+
+extern "C" int dimgpu_static_scratch_status(void* stream) {
+    using namespace dimgpu;
+    dimgpu_calibrator cal;
+    DG_CHECK(static_calibrator(nullptr, &cal));
+    uint32_t st = 0;
+    DG_CHECK(take_status_word(cal.status, static_cast<cudaStream_t>(stream), &st));
+    return status_error(st, "static-scratch SpMV");
+}
+
+extern "C" int dimgpu_csr5_status(const dimgpu_csr5* m, dimgpu_calibrator* cal, void* stream) {
+    using namespace dimgpu;
+    if (!m && !cal)
+        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "NULL matrix and calibrator");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint32_t st = 0;
+    if (cal) {
+        DG_CHECK(take_status_word(cal->status, s, &st));
+        return status_error(st, "SpMV (caller's calibrator)");
+    }
+    // the scratch the matrix owns: its calibrator, its SpMM scratch, and those of its cached transpose
+    uint32_t first = kStatusOk;
+    const char* where = "";
+    for (const dimgpu_csr5* h = m; h; h = h->transposed) {
+        const char* names[2] = {h == m ? "SpMV (matrix calibrator)" : "transpose SpMV",
+                                h == m ? "SpMM" : "transpose SpMM"};
+        uint32_t* words[2] = {h->own_cal ? h->own_cal->status : nullptr,
+                              h->spmm_sc ? static_cast<spmm_scratch*>(h->spmm_sc)->status : nullptr};
+        for (int i = 0; i < 2; ++i) {
+            DG_CHECK(take_status_word(words[i], s, &st));
+            if (st != kStatusOk && first == kStatusOk) {
+                first = st;
+                where = names[i];
+            }
+        }
+    }
+    return status_error(first, where);
+}
+
+#ifdef DIMGPU_TEST_HOOKS
+// Test builds only (libdimgpu_test.so, compiled with a short DIMGPU_WAIT_NS): the next SpMV launches
+// leave the look-back flag of warp run `run` unwritten, so that a later run's bounded wait expires
+// (0xffffffff restores normal launches).
+extern "C" DIMGPU_API void dimgpu_test_withhold_run(uint32_t run) { dimgpu::g_test_withhold_run = run; }
+
+// Test builds only: gives the matrix's f64 SpMV plan `grid` CTAs (no launch is made with it; the
+// static-scratch entry point must refuse a plan larger than its slots).
+extern "C" DIMGPU_API int dimgpu_test_set_spmv_grid(dimgpu_csr5* m, int grid) {
+    if (!m || grid < 1)
+        return DIMGPU_ERR_INVALID_ARGUMENT;
+    m->plan.grid = grid;
+    m->plan.nwarps = (uint32_t)grid * (uint32_t)m->plan.warps_per_cta;
+    return DIMGPU_OK;
+}
+#endif

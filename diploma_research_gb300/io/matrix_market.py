@@ -7,7 +7,7 @@ Mirrors ``dim::io::matrix_market`` (include/dim/io/matrix_market.h:25-83):
 * ``pattern`` matrices get value 1.0 (matrix_market.h:33-34);
 * indices are made 0-based (matrix_market.h:44-46);
 * ``symmetric`` / ``hermitian`` matrices are expanded when converting to CSR, the mirrored entry
-  being emitted right after its source entry (coo.h:126-139);
+  being emitted right after its source entry (coo.h:33-46);
 * ``load_as_csr`` = ``load_as_coo`` + ``csr.from_coo`` (matrix_market.h:68-73).
 """
 from __future__ import annotations

@@ -30,7 +30,7 @@ class coo:
         self.symmetric = bool(symmetric)
 
     def expanded(self):
-        """(values, rows, cols) in the order ``coo::iterate`` visits them (coo.h:126-139)."""
+        """(values, rows, cols) in the order ``coo::iterate`` visits them (coo.h:33-46)."""
         v, r, c = self.values, self.row_indices, self.col_indices
         if not self.symmetric:
             return v, r, c

@@ -140,11 +140,31 @@ DIMGPU_API int dimgpu_csr5_set_spmv_launch(dimgpu_csr5* m, int f32, uint32_t war
  *   - Limit: matrices whose SpMV launch uses more than 4096 warp slots (more than 256 SMs x 16
  *     warps) are rejected with DIMGPU_ERR_INVALID_ARGUMENT.
  *   - The first call on a device looks up the array's device address (cudaGetSymbolAddress) with
- *     that device current; make that first call before any stream capture.
+ *     that device current, and so does the first call in a new context of that device (after
+ *     cudaDeviceReset, for instance); make that first call before any stream capture.
  *   - Every call on a device shares the one array: calls that overlap on the GPU (different streams,
  *     or concurrent graph branches) race and give wrong results.  Calls in one stream are safe.
+ *   - A device-side failure (an expired bounded wait, an inconsistent format) is kept in the array's
+ *     status word, which calls do not clear; dimgpu_static_scratch_status reads and clears it.
  *   - x, y: device memory of the matrix's device (the current device).  The call is asynchronous. */
 DIMGPU_API int dimgpu_csr5_spmv_static_scratch(const dimgpu_csr5* m, const double* x, double* y, void* stream);
+
+/* ---- device-side failures of asynchronous calls ------------------------------------------------ */
+
+/* The asynchronous entry points (dimgpu_csr5_spmv, _spmv_dot, _spmv_f32, _spmm, _spmm_f32,
+ * _spmv_transpose) return before their kernels run.  A kernel that meets a failure -- a bounded device
+ * wait that expired, or a consistency check on the CSR5 arrays that failed -- records it in the status
+ * word of the scratch it ran on and leaves its outputs invalid.  These calls synchronize `stream`, then
+ * read and clear that word: DIMGPU_OK (no failure since the last query), DIMGPU_ERR_TIMEOUT or
+ * DIMGPU_ERR_BAD_INDEX.  The reference reports its failures synchronously by exception
+ * (std::invalid_argument, csr5.h:820-821); the _host entry points and the CG solvers read the word
+ * themselves and return the code directly.
+ *
+ * cal != NULL: the calibrator the products ran on.  cal == NULL: the scratch matrix m owns (its own
+ * calibrator, used when a product is given cal = NULL; its SpMM scratch; those of its cached A^T). */
+DIMGPU_API int dimgpu_csr5_status(const dimgpu_csr5* m, dimgpu_calibrator* cal, void* stream);
+/* The same for the static scratch of dimgpu_csr5_spmv_static_scratch on the current device. */
+DIMGPU_API int dimgpu_static_scratch_status(void* stream);
 
 /* ---- several right-hand sides ------------------------------------------------------------------- */
 
@@ -248,7 +268,7 @@ DIMGPU_API int dimgpu_cg_adjoint(const dimgpu_csr5* m, const double* g, const do
 /* ---- diagnostics ------------------------------------------------------------------------------ */
 
 DIMGPU_API const char* dimgpu_last_error_string(void);
-/* Device status word of the last kernel that reported one (0 = none); cleared by this call. */
+/* ABI version of this library. */
 DIMGPU_API int dimgpu_version(void);
 
 #ifdef __cplusplus

@@ -42,13 +42,18 @@ def build(ref: bool = False) -> None:
     """Compile the restatement (and, if asked and possible, the reference shim)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
     if ref and ref_buildable():
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={os.path.abspath(ref_root())}"], check=True)
+
+
+def ref_root() -> str:
+    """The reference checkout: $REF_ROOT, else a `reference` directory beside the repository."""
+    return os.environ.get("REF_ROOT", os.path.join(os.path.dirname(HERE), os.pardir, "reference"))
 
 
 def ref_buildable() -> bool:
     import platform
 
-    root = os.environ.get("REF_ROOT", "/root/reference")
+    root = ref_root()
     return platform.machine() in ("x86_64", "AMD64") and os.path.isfile(
         os.path.join(root, "include", "dim", "mat", "storage_formats", "csr5.h"))
 
@@ -208,7 +213,8 @@ def ref():
             if not os.path.isfile(REF_SO):
                 if not ref_buildable():
                     return None
-                subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+                subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={os.path.abspath(ref_root())}"],
+                               check=True)
             L = ctypes.CDLL(REF_SO)
             L.dimref_csr5_from_csr.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p,
                                                _f64p]
@@ -223,8 +229,35 @@ def ref():
                                     ctypes.POINTER(ctypes.c_double)]
             L.dimref_cg.restype = ctypes.c_int64
             L.dimref_max_threads.restype = ctypes.c_int
+            L.dimref_csr_from_coo.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, _f64p, _u32p, _u32p,
+                                              ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
+            L.dimref_csr_from_coo.restype = ctypes.c_void_p
+            L.dimref_csr_export.argtypes = [ctypes.c_void_p, _u32p, _u32p, _f64p]
+            L.dimref_csr_free.argtypes = [ctypes.c_void_p]
             _ref = L
     return _ref
+
+
+def ref_csr_from_coo(rows, cols, values, row_indices, col_indices, symmetric=False):
+    """The reference's csr<double>::from_coo (csr.h:42-77) of a coo (coo.h:17-47); returns
+    (row_start_offsets, col_indices, values)."""
+    L = ref()
+    if L is None:
+        raise RuntimeError("reference shim unavailable on this host")
+    v, r, c = _f64(values), _u32(row_indices), _u32(col_indices)
+    pad = lambda a, dt: a if a.size else np.zeros(1, dt)
+    nnz_out = ctypes.c_uint64()
+    h = L.dimref_csr_from_coo(int(rows), int(cols), v.size, pad(v, np.float64), pad(r, np.uint32),
+                              pad(c, np.uint32), 1 if symmetric else 0, ctypes.byref(nnz_out))
+    try:
+        k = int(nnz_out.value)
+        rp = np.zeros(int(rows) + 1, np.uint32)
+        ci = np.zeros(max(1, k), np.uint32)
+        vv = np.zeros(max(1, k), np.float64)
+        L.dimref_csr_export(h, rp, ci, vv)
+        return rp, ci[:k], vv[:k]
+    finally:
+        L.dimref_csr_free(h)
 
 
 class RefCSR5:

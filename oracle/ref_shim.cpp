@@ -8,6 +8,8 @@
 //
 // Every SpMV here follows the oracle rule: y zero-filled and a fresh calibrator per call
 // (csr5.h:530,744-745 and csr5/calibrator.h:14-31 make the reference drift otherwise).
+#include <dim/mat/storage_formats/coo.h>
+#include <dim/mat/storage_formats/csr.h>
 #include <dim/mat/storage_formats/csr5.h>
 #include <dim/vec.h>
 
@@ -22,16 +24,45 @@
 namespace {
 using csr_t = dim::mat::csr<double>;
 using csr5_t = dim::mat::csr5<double>;
+using coo_t = dim::mat::coo<double>;
 
 struct handle_t
 {
     csr5_t m;
+};
+
+struct csr_handle_t
+{
+    csr_t m;
 };
 } // namespace
 
 extern "C" {
 
 int dimref_max_threads() { return omp_get_max_threads(); }
+
+// csr<double>::from_coo (csr.h:42-77) of a coo (coo.h:17-47) holding the caller's triplets; with
+// symmetric != 0 the coo stands for its mirror entries too (coo::iterate, coo.h:33-46).  *out_nnz gets
+// the CSR's non-zero count; dimref_csr_export copies the arrays out.
+void* dimref_csr_from_coo(uint32_t rows, uint32_t cols, uint64_t nnz, const double* val, const uint32_t* row,
+                          const uint32_t* col, int symmetric, uint64_t* out_nnz) {
+    coo_t coo{dim::mat::dimensions_t{.rows = rows, .cols = cols}, nnz, symmetric != 0};
+    std::copy(val, val + nnz, coo.values.begin());
+    std::copy(row, row + nnz, coo.row_indices.begin());
+    std::copy(col, col + nnz, coo.col_indices.begin());
+    auto* h = new csr_handle_t{csr_t::from_coo(coo)};
+    *out_nnz = h->m.values.size();
+    return h;
+}
+
+void dimref_csr_export(void* h, uint32_t* row_ptr, uint32_t* col, double* val) {
+    const auto& m = static_cast<csr_handle_t*>(h)->m;
+    std::copy(m.row_start_offsets.begin(), m.row_start_offsets.end(), row_ptr);
+    std::copy(m.col_indices.begin(), m.col_indices.end(), col);
+    std::copy(m.values.begin(), m.values.end(), val);
+}
+
+void dimref_csr_free(void* h) { delete static_cast<csr_handle_t*>(h); }
 
 // csr5<double,16,4,uint32_t>::from_csr (csr5.h:791-803) on copies of the caller's CSR arrays.
 void* dimref_csr5_from_csr(uint32_t rows, uint32_t cols, uint64_t nnz, const uint32_t* row_ptr, const uint32_t* col,

@@ -34,3 +34,15 @@ def native():
     from diploma_research_gb300 import _native as N
 
     return N.lib()
+
+
+@pytest.fixture(scope="session")
+def native_test():
+    """libdimgpu_test.so: the library built with test hooks and 20 ms bounded device waits (only for the
+    tests that make a wait run out)."""
+    from diploma_research_gb300 import build as B
+
+    B.build(variant="test")
+    from diploma_research_gb300 import _native as N
+
+    return N.test_lib()

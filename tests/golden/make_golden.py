@@ -1,6 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a checkout that has the reference at REF_ROOT (default /root/reference) on an x86-64 host:
+Run on an x86-64 host with the reference checkout at REF_ROOT (default: a `reference` directory beside
+the repository):
 
     python tests/golden/make_golden.py
 
@@ -11,6 +12,9 @@ Run in a checkout that has the reference at REF_ROOT (default /root/reference) o
   seeded x (oracle rule: zeroed y, fresh calibrator).
 * ``ref_cases.npz`` -- small seeded matrices (random lengths, empty rows, long rows, a dense row,
   rows spanning tiles) with the reference's conversion arrays, SpMV outputs and CG iterates.
+* ``coo_cases.npz`` -- COO inputs and what the reference's csr::from_coo (csr.h:42-77) makes of them:
+  mm.mtx as read, a symmetric COO (lower triangle, expanded by coo::iterate, coo.h:33-46), short rows
+  with duplicate coordinates, and long unsorted rows with duplicates.
 
 The reference runs through oracle/ref_shim.cpp compiled against the reference headers
 (``make -C oracle ref``).
@@ -27,9 +31,9 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 import oracle  # noqa: E402
-from diploma_research_gb300.io.matrix_market import load_as_csr  # noqa: E402
+from diploma_research_gb300.io.matrix_market import load_as_coo, load_as_csr  # noqa: E402
 
-REF_ROOT = os.environ.get("REF_ROOT", "/root/reference")
+REF_ROOT = oracle.ref_root()
 
 
 def ref_arrays(rows, cols, rp, ci, v):
@@ -55,6 +59,10 @@ def random_case(rng, rows, cols, density, empty_frac=0.0, long_rows=0, dense_row
 
 
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "coo":
+        if oracle.ref() is None:
+            raise SystemExit("the reference shim cannot be built on this host")
+        return coo_cases()
     if oracle.ref() is None:
         raise SystemExit("the reference shim cannot be built on this host")
     # ---- mm.mtx ----
@@ -110,6 +118,44 @@ def main():
     out["ref_threads"] = oracle.RefCSR5.max_threads()
     np.savez_compressed(os.path.join(HERE, "ref_cases.npz"), **out)
     print("wrote mm_mtx.npz and ref_cases.npz; cases", cases, "cg iters", it)
+    coo_cases()
+
+
+def coo_cases():
+    """COO -> CSR through the reference's csr::from_coo, on four inputs (see the module docstring)."""
+    rng = np.random.default_rng(20261204)
+    cases = {}
+    c = load_as_coo(os.path.join(REF_ROOT, "tests", "test_files", "mm.mtx"))
+    cases["mm"] = (c.dimensions.rows, c.dimensions.cols, c.values, c.row_indices, c.col_indices, False)
+    # symmetric: lower triangle with the diagonal, shuffled entry order
+    n = 400
+    rows = rng.integers(0, n, 3000)
+    cols = rng.integers(0, n, 3000)
+    lo = np.minimum(rows, cols), np.maximum(rows, cols)
+    key = np.unique(lo[1] * n + lo[0])
+    r, cc = key // n, key % n
+    perm = rng.permutation(key.size)
+    cases["symmetric"] = (n, n, rng.standard_normal(key.size)[perm], r[perm], cc[perm], True)
+    # short rows (< 16 elements) with duplicate coordinates
+    n = 300
+    r = rng.integers(0, n, 1800)
+    cc = rng.integers(0, 40, 1800)
+    cases["dups_short"] = (n, 40, rng.standard_normal(r.size), r, cc, False)
+    # long rows with duplicates, entries in random order
+    n = 30
+    r = rng.integers(0, n, 4000)
+    cc = rng.integers(0, 300, 4000)
+    cases["dups_long"] = (n, 300, rng.standard_normal(r.size), r, cc, False)
+    out = {}
+    for name, (nr, nc, v, r, cc, sym) in cases.items():
+        rp, ci, vv = oracle.ref_csr_from_coo(nr, nc, v, r, cc, symmetric=sym)
+        out.update({f"{name}_rows": nr, f"{name}_cols": nc, f"{name}_v": np.asarray(v, np.float64),
+                    f"{name}_r": np.asarray(r, np.uint32), f"{name}_c": np.asarray(cc, np.uint32),
+                    f"{name}_symmetric": sym, f"{name}_ref_row_ptr": rp, f"{name}_ref_col": ci,
+                    f"{name}_ref_val": vv})
+    out["cases"] = np.array(list(cases))
+    np.savez_compressed(os.path.join(HERE, "coo_cases.npz"), **out)
+    print("wrote coo_cases.npz:", list(cases))
 
 
 if __name__ == "__main__":

@@ -45,3 +45,15 @@ def assert_spmv_close(y, y_ref, absax, rtol):
     bad = np.flatnonzero(err > bound)
     assert bad.size == 0, (f"{bad.size} rows exceed {rtol} * (|A||x|): first {bad[:5]}, "
                            f"err {err[bad[:5]]}, bound {bound[bad[:5]]}")
+
+
+def record(case: str, **values):
+    """Appends one JSON line {case, values} to the file named by DIMGPU_TEST_RECORD (when set), so that a
+    run can keep the measured errors and iteration counts of the full-size parity cases."""
+    import json
+    import os
+
+    path = os.environ.get("DIMGPU_TEST_RECORD")
+    if path:
+        with open(path, "a") as fh:
+            fh.write(json.dumps({"case": case, **values}) + "\n")

@@ -16,8 +16,19 @@ def test_builds_and_exports_every_declared_symbol(native):
     out = subprocess.run(["nm", "-D", "--defined-only", N.LIB_PATH], capture_output=True, text=True).stdout
     exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
     assert set(declared) <= exported
-    # nothing else leaks from the library's C++ internals
+    # nothing else leaks from the library's C++ internals, and the test hooks are not in the product
     assert all(s.startswith("dimgpu_") for s in exported if not s.startswith("_"))
+    assert not any(s.startswith("dimgpu_test_") for s in exported)
+
+
+def test_test_library_adds_only_the_hooks(native_test):
+    """libdimgpu_test.so exports the product's entry points plus the two test hooks."""
+    declared = set(N.declared_symbols())
+    out = subprocess.run(["nm", "-D", "--defined-only", N.TEST_LIB_PATH], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    assert declared <= exported
+    assert {s for s in exported if s.startswith("dimgpu_test_")} == {"dimgpu_test_withhold_run",
+                                                                    "dimgpu_test_set_spmv_grid"}
 
 
 def test_argument_errors_without_device(native):
@@ -41,6 +52,7 @@ def test_argument_errors_without_device(native):
     # NULL matrix
     assert native.dimgpu_csr5_spmv(None, None, None, None, None) == N.ERR_INVALID_ARGUMENT
     assert native.dimgpu_cg_create(None, None, None, None) == N.ERR_INVALID_ARGUMENT
+    assert native.dimgpu_csr5_status(None, None, None) == N.ERR_INVALID_ARGUMENT
     assert native.dimgpu_version() == 1
 
 
