@@ -218,7 +218,7 @@ def run_gpu(args):
     stream = torch.cuda.current_stream()
     bd = torch.tensor(b, device="cuda", dtype=torch.float64)
     xd = torch.zeros(n, device="cuda", dtype=torch.float64)
-    s64 = CGSolver(A, tol=TOL, precision="fp64", stream=stream, use_graph=not args.no_graph)
+    s64 = CGSolver(A, tol=TOL, precision="fp64", stream=stream, use_graph=not args.no_graph, engine=args.engine)
     smx = CGSolver(A, tol=TOL, precision="mixed", stream=stream, use_graph=not args.no_graph)
 
     def solve(solver):
@@ -384,7 +384,9 @@ def run_gpu(args):
 
 
 def run_spmv_only(args):
-    """A short SpMV-only run (few launches) for profiler captures: 5 warm-up + `steps` launches."""
+    """A short SpMV-only run (few launches) for profiler captures: 5 warm-up + `steps` launches.
+    --layout hub_first runs it on the matrix renumbered by decreasing row length (csr.hub_first_order);
+    --all-launches times every launch configuration instead (30 launches each)."""
     import numpy as np
     import torch
 
@@ -394,8 +396,12 @@ def run_spmv_only(args):
     from diploma_research_gb300.csr5 import csr5
 
     m, _, _ = _workload()
+    if args.layout == "hub_first":
+        m = m.permuted(m.hub_first_order())
     n, nnz = m.dimensions.rows, m.nnz
     A = csr5.from_csr(m)
+    if args.all_launches:
+        return _time_all_launches(A, n)
     stream = torch.cuda.current_stream()
     dt = torch.float32 if args.f32 else torch.float64
     x = torch.tensor(np.random.default_rng(5).uniform(-1, 1, n), device="cuda", dtype=dt)
@@ -414,6 +420,35 @@ def run_spmv_only(args):
     nbytes = (8 * nnz + 8 * n) if args.f32 else (12 * nnz + 16 * n)
     print(json.dumps({"spmv_seconds": s, "gbps": nbytes / s / 1e9, "nnz": nnz, "n": n, "f32": bool(args.f32),
                       "launch": A.spmv_launch(bool(args.f32))}))
+    return 0
+
+
+def _time_all_launches(A, n):
+    """CUDA-event time of the f64 and f32 SpMV in every launch configuration (warps per CTA x gathers)."""
+    import numpy as np
+    import torch
+
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    x = torch.tensor(np.random.default_rng(5).uniform(-1, 1, n), device="cuda", dtype=torch.float64)
+    y = torch.empty(n, device="cuda", dtype=torch.float64)
+    x32, y32 = x.float(), torch.empty(n, device="cuda", dtype=torch.float32)
+    out = {"chosen_f64": A.spmv_launch(False), "chosen_f32": A.spmv_launch(True)}
+    for f32, wpcs in ((False, (16, 12)), (True, (24, 20))):
+        xx, yy = (x32, y32) if f32 else (x, y)
+        for w in wpcs:
+            for g in ("l1", "stream"):
+                A.set_spmv_launch(w, g, f32=f32)
+                for _ in range(5):
+                    A.spmv(xx, yy)
+                torch.cuda.synchronize()
+                ev0.record(stream)
+                for _ in range(30):
+                    A.spmv(xx, yy)
+                ev1.record(stream)
+                torch.cuda.synchronize()
+                out[f"{'f32' if f32 else 'f64'}_{w}_{g}_us"] = ev0.elapsed_time(ev1) / 30 * 1e3
+    print(json.dumps(out))
     return 0
 
 
@@ -455,7 +490,7 @@ def run_spmm_only(args):
 def run_batch(args):
     """Multi-RHS workload: 3-D 7-point Laplacian 192^3 (n = 7,077,888), k right-hand sides b_j = A x*_j
     (x* ~ U[-1,1], seed 3), block CG to 1e-10 per column in FP64 and mixed precision, against k separate
-    FP64 solves (timed on two columns and scaled by k/2).  Prints one JSON line per k."""
+    FP64 solves (each column solved and timed).  Prints one JSON line per k."""
     import numpy as np
     import torch
 
@@ -463,7 +498,7 @@ def run_batch(args):
 
     B.build()
     from diploma_research_gb300.cg import BlockCGSolver, CGSolver
-    from diploma_research_gb300.csr5 import csr5
+    from diploma_research_gb300.csr5 import csr5, spmm_shape
     from diploma_research_gb300.generators import WORKLOADS, rhs
 
     m = WORKLOADS["lap3d7_192"]["build"]()
@@ -489,9 +524,10 @@ def run_batch(args):
             out[prec] = {"seconds": sec, "rhs_solves_per_s": k / sec, "iterations": res.iterations,
                          "converged_columns": res.converged_columns, "max_rel_residual": res.max_rel_residual,
                          "reliable_updates": res.reliable_updates, "rel_error_vs_xstar": err}
+            out[prec]["spmm_shape"] = spmm_shape(A, min(k, 32), prec == "mixed")
             del s
         sep = []
-        for j in range(min(2, k)):
+        for j in range(k):
             b = torch.tensor(np.ascontiguousarray(Bh[:, j]), device="cuda", dtype=torch.float64)
             x = torch.zeros(n, device="cuda", dtype=torch.float64)
             single.solve(b, x, stream=stream)
@@ -501,9 +537,9 @@ def run_batch(args):
             _, r1 = single.solve(b, x, stream=stream)
             torch.cuda.synchronize()
             sep.append((time.perf_counter() - t, r1.iterations))
-        sep_s = statistics.mean(v[0] for v in sep) * k
+        sep_s = sum(v[0] for v in sep)
         out["separate_fp64"] = {"seconds": sep_s, "rhs_solves_per_s": k / sep_s,
-                                "iterations": [v[1] for v in sep], "note": "two columns timed, scaled to k"}
+                                "iterations": [v[1] for v in sep], "note": "all k columns solved one after another"}
         out["speedup_block_fp64"] = sep_s / out["fp64"]["seconds"]
         out["speedup_block_mixed"] = sep_s / out["mixed"]["seconds"]
         print(json.dumps(out), flush=True)
@@ -554,13 +590,15 @@ def run_adjoint(args):
             lam = torch.zeros(n, device="cuda", dtype=torch.float64)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            _, rf = fwd.solve(b, x, stream=stream)
+            _, rf = fwd.solve(b, x, stream=stream, raise_on_failure=False)
             g = 2.0 * (x - xtd)
-            ra = cg_adjoint(A, g, x, lam, gv, tol=TOL, precision=prec, stream=stream)
+            ra = cg_adjoint(A, g, x, lam, gv, tol=TOL, precision=prec, stream=stream, raise_on_failure=False,
+                            **({"reliable_delta": args.reliable_delta} if args.reliable_delta else {}))
             torch.cuda.synchronize()
             sec = time.perf_counter() - t0
         results[prec] = (x, lam, gv)
         out[prec] = {"seconds": sec, "forward_iterations": rf.iterations, "adjoint_iterations": ra.iterations,
+                     "forward_converged": rf.converged, "adjoint_converged": ra.converged,
                      "forward_rel_residual": rf.rel_residual, "adjoint_rel_residual": ra.rel_residual,
                      "forward_seconds_device": rf.seconds, "adjoint_seconds_device": ra.seconds}
     # adjoint identity on random directions (FP64 forward solves to 1e-12 give the right-hand sides)
@@ -590,6 +628,24 @@ def run_adjoint(args):
     lam64, lamx = results["fp64"][1], results["mixed"][1]
     out["mixed_vs_fp64_lambda_rel_error"] = float(torch.linalg.norm(lamx - lam64) / torch.linalg.norm(lam64))
     out["mixed_speedup"] = out["fp64"]["seconds"] / out["mixed"]["seconds"]
+    # the FP64 CPU adjoint: one sparse LU factorisation of A gives x = A^-1 b and lambda = A^-T g
+    import scipy.sparse.linalg as spla
+
+    t = time.perf_counter()
+    lu = spla.splu(Sd.tocsc(), permc_spec="MMD_AT_PLUS_A")
+    x_ref = lu.solve(bh)
+    lam_ref = lu.solve(2.0 * (x_ref - xt), trans="T")
+    rows = np.repeat(np.arange(n), np.diff(m.row_start_offsets.astype(np.int64)))
+    gv_ref = -lam_ref[rows] * x_ref[m.col_indices]
+    out["cpu_adjoint_seconds"] = time.perf_counter() - t
+    rel = lambda a, r: float(np.linalg.norm(a - r) / np.linalg.norm(r))
+    for prec in ("fp64", "mixed"):
+        x, lam, gv = results[prec]
+        out[prec]["rel_error_x_vs_cpu"] = rel(x.cpu().numpy(), x_ref)
+        out[prec]["rel_error_lambda_vs_cpu"] = rel(lam.cpu().numpy(), lam_ref)
+        out[prec]["rel_error_grad_vals_vs_cpu"] = rel(gv.cpu().numpy(), gv_ref)
+    out["tol"] = TOL
+    out["reliable_delta"] = args.reliable_delta
     print(json.dumps(out), flush=True)
     return 0
 
@@ -605,16 +661,26 @@ def main():
     ap.add_argument("--spmm-only", type=int, default=0, metavar="K",
                     help="few SpMM launches with K right-hand sides only (for profiler captures)")
     ap.add_argument("--f32", action="store_true", help="with --spmv-only / --spmm-only: the f32 product")
+    ap.add_argument("--layout", default="as_generated", choices=["as_generated", "hub_first"],
+                    help="with --spmv-only: the matrix as generated or renumbered by decreasing row length")
+    ap.add_argument("--all-launches", action="store_true",
+                    help="with --spmv-only: time the f64 and f32 SpMV in every launch configuration")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven CG loop instead of the CUDA graph (profilers list every kernel)")
+    ap.add_argument("--engine", default="auto", choices=["auto", "graph", "merged"],
+                    help="CG engine of the FP64 solve (the mixed solve always runs the graph engine)")
     ap.add_argument("--batch", default=None, help="comma-separated k: the multi-RHS block-CG workload")
     ap.add_argument("--adjoint", action="store_true", help="the differentiable-solve workload (adjoint CG)")
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(DESCR),
                     help="the system of the CG comparison (default: the 27-point 128^3 stencil)")
+    ap.add_argument("--tol", type=float, default=None,
+                    help="relative residual to solve to (default: the workload's, 1e-8 for lap2d_512, else 1e-10)")
+    ap.add_argument("--reliable-delta", type=float, default=None,
+                    help="with --adjoint: the mixed adjoint solve's residual drop between f64 replacements")
     args = ap.parse_args()
     globals()["WORKLOAD"] = args.workload
-    globals()["TOL"] = __import__("diploma_research_gb300.generators", fromlist=["WORKLOADS"]).WORKLOADS[
-        args.workload]["tol"]
+    globals()["TOL"] = args.tol if args.tol is not None else __import__(
+        "diploma_research_gb300.generators", fromlist=["WORKLOADS"]).WORKLOADS[args.workload]["tol"]
     if args.adjoint:
         return run_adjoint(args)
     if args.batch:

@@ -54,7 +54,7 @@ class cg_params(ctypes.Structure):
                 ("use_graph", ctypes.c_int32), ("reliable_delta", ctypes.c_double), ("engine", ctypes.c_int32)]
 
 
-CG_ENGINE_AUTO, CG_ENGINE_GRAPH, CG_ENGINE_FUSED = 0, 1, 2
+CG_ENGINE_AUTO, CG_ENGINE_GRAPH, CG_ENGINE_MERGED = 0, 1, 2
 
 
 class cg_stats(ctypes.Structure):
@@ -111,6 +111,7 @@ _SIGNATURES = {
     "dimgpu_csr5_spmm": [_vp, _u32, _vp, _u64, _vp, _u64, _vp],
     "dimgpu_csr5_spmm_f32": [_vp, _u32, _vp, _u64, _vp, _u64, _vp],
     "dimgpu_csr5_spmm_shape": [_vp, _u32, ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
+    "dimgpu_csr5_set_spmm_shape": [_vp, _u32, ctypes.c_int, ctypes.c_int],
     "dimgpu_vec_axpy": [_u64, _f64, _vp, _vp, _vp],
     "dimgpu_vec_aypx": [_u64, _f64, _vp, _vp, _vp],
     "dimgpu_vec_set": [_u64, _f64, _vp, _vp],

@@ -28,10 +28,14 @@ def pattern_outer(A: csr5, u, v, scale, out, stream=None):
 
 
 def cg_adjoint(A: csr5, g, x, lam, grad_vals=None, tol: float = 1e-10, max_it: int = 100000,
-               precision: str = "fp64", stream=None, raise_on_failure: bool = True):
+               precision: str = "fp64", stream=None, raise_on_failure: bool = True, reliable_delta: float = 0.1,
+               engine: str = "auto"):
     """lambda := A^{-T} g by CG on A^T (lam holds the initial guess), grad_vals := -lambda x^T on the
-    pattern.  Returns cg_result of the adjoint solve."""
-    p = N.cg_params(float(tol), int(max_it), _PREC[precision], 1, 0.1, N.CG_ENGINE_AUTO)
+    pattern.  Returns cg_result of the adjoint solve.  reliable_delta: mixed precision only (the residual
+    drop between f64 residual replacements)."""
+    from .cg import _ENGINE
+
+    p = N.cg_params(float(tol), int(max_it), _PREC[precision], 1, float(reliable_delta), _ENGINE[engine])
     st = N.cg_stats()
     rc = N.lib().dimgpu_cg_adjoint(A._h, N.device_ptr(g, "<f8"), N.device_ptr(x, "<f8"), N.device_ptr(lam, "<f8"),
                                    N.device_ptr(grad_vals, "<f8") if grad_vals is not None else None,

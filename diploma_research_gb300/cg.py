@@ -29,13 +29,13 @@ class cg_result:
 
 
 _PREC = {"fp64": N.CG_FP64, "mixed": N.CG_MIXED}
-_ENGINE = {"auto": N.CG_ENGINE_AUTO, "graph": N.CG_ENGINE_GRAPH, "fused": N.CG_ENGINE_FUSED}
+_ENGINE = {"auto": N.CG_ENGINE_AUTO, "graph": N.CG_ENGINE_GRAPH, "merged": N.CG_ENGINE_MERGED}
 
 
 class CGSolver:
     """engine: "auto" (the library's choice, currently the graph), "graph" (one CUDA graph, three kernels
-    per iteration) or "fused" (one persistent cooperative kernel per solve); use_graph=False runs the
-    host-driven loop of kernels."""
+    per iteration, the reference's recurrence) or "merged" (FP64 only: the Chronopoulos-Gear recurrence,
+    two kernels per iteration); use_graph=False runs the same kernels from a host-driven loop."""
 
     def __init__(self, A: csr5, tol: float = 1e-10, max_it: int = 100000, precision: str = "fp64",
                  use_graph: bool = True, reliable_delta: float = 0.03, stream=None, engine: str = "auto"):

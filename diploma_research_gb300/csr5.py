@@ -274,7 +274,13 @@ def spmm(A: csr5, X, Y, stream=None):
 
 
 def spmm_shape(A: csr5, k: int, f32: bool = False) -> int:
-    """The autotuned SpMM launch shape for (k, precision), -1 before the first call."""
+    """The autotuned SpMM shape for (k, precision), -1 before the first call: bit 0 the launch shape,
+    bits 1-2 the lane grouping (see dimgpu_csr5_spmm_shape in include/dimgpu.h)."""
     v = ctypes.c_int()
     N.check(N.lib().dimgpu_csr5_spmm_shape(A._h, k, 1 if f32 else 0, ctypes.byref(v)))
     return int(v.value)
+
+
+def set_spmm_shape(A: csr5, k: int, shape: int, f32: bool = False) -> None:
+    """Pins the SpMM shape for (k, precision) (0..5, or -1 to re-tune on the next call)."""
+    N.check(N.lib().dimgpu_csr5_set_spmm_shape(A._h, k, 1 if f32 else 0, int(shape)))

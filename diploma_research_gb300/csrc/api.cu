@@ -157,7 +157,7 @@ extern "C" {
 
 const char* dimgpu_last_error_string(void) { return g_last_error.c_str(); }
 
-int dimgpu_version(void) { return 1; }
+int dimgpu_version(void) { return 2; }
 
 int dimgpu_csr5_from_csr(uint32_t rows, uint32_t cols, uint64_t nnz, const uint32_t* row_ptr, const uint32_t* col_idx,
                          const double* vals, int mem, const dimgpu_csr5_options* opt, void* stream,

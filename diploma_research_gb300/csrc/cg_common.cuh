@@ -1,12 +1,12 @@
-// cg_common.cuh -- state shared by the CG drivers: the graph-driven kernels (cg.cu) and the persistent
-// cooperative kernel (cg_fused.cu).
+// cg_common.cuh -- the device-resident state of one CG solve, shared by the CG kernels (cg.cu) and the
+// SpMV epilogue that computes the step lengths (spmv.cu).
 #pragma once
 
 #include <cuda_runtime.h>
 
 #include <cstdint>
 
-struct dimgpu_csr5;
+#include "common.cuh"
 
 namespace dimgpu {
 
@@ -21,6 +21,7 @@ struct cg_state {
     double maxrr;    // mixed: largest r.r since the last reliable update
     double delta2;   // mixed: reliable_delta^2
     double rr_true;  // last true residual r.r (f64)
+    double rr_prev;  // merged engine: r.r of the previous residual
     int64_t iter, max_it, ru_count;
     uint32_t stop;       // the solve has finished
     uint32_t x_pending;  // f64: kernel C owes x += alpha s
@@ -28,48 +29,29 @@ struct cg_state {
     uint32_t converged;
 };
 
-// Everything the persistent CG kernel touches.  The matrix is in the device layout (omega = 32,
-// sigma = 16); the f32 fields are used by the mixed solver only.
-struct cg_fused_args {
-    // matrix
-    const double* vals;
-    const float* vals32;
-    const uint32_t* col;
-    const uint32_t* desc;
-    const uint32_t* tile_ptr;
-    const uint32_t* tdo_ptr;
-    const uint32_t* tdo;
-    const uint32_t* row_ptr;
-    uint64_t T;
-    uint32_t rows;
-    uint32_t tail_start;
-    uint64_t tpw;        // tiles per warp
-    uint32_t nwarps;     // grid * warps per CTA
-    uint32_t tail_warp;  // the warp that owns the last tile and computes the CSR tail
-    int keep_matrix;     // the matrix stays in L2 between products
-    // vectors (n = rows)
-    const double* b;
-    double *x, *r, *s, *As, *Ax;
-    float *r32, *s32, *As32, *y32;
-    // scratch
-    double* cal_val;    // [nwarps] each warp's head fragment
-    uint32_t* cal_row;  // [nwarps] its row | kDirty when valid
-    uint32_t* flag;     // [nwarps] (phase << 1) | through, published after the warp's tiles
-    double* part;       // [3][grid][2] per-CTA partial sums
-    uint32_t* bar;      // grid barrier: [0] arrivals, [32] generation
-    uint32_t* status;
-    cg_state* st;
-    // parameters
-    double tol2, delta2;
-    int64_t max_it;
-    int mixed;
-    int grid;
-};
-
-// cg_fused.cu: the grid the persistent kernel runs with on this matrix's device (an error when the device
-// cannot run it), the number of warps of that grid, and the launch.
-int cg_fused_grid(const struct ::dimgpu_csr5* m, int* grid);
-uint32_t cg_fused_warps(int grid);
-int launch_cg_fused(const cg_fused_args& a, cudaStream_t stream);
+// Step lengths of the merged (Chronopoulos-Gear) recurrence, computed by the SpMV's last CTA once
+// delta = r.w (w = A r) is known, with gamma = r.r from the vector kernel before it:
+//   first iteration  beta = 0, alpha = gamma / delta
+//   otherwise        beta = gamma / gamma_prev, alpha = gamma / (delta - beta gamma / alpha_prev)
+// The denominator is p.Ap of the new direction; a non-positive or non-finite one is a breakdown (the
+// matrix is not SPD), which stops the solve.
+__device__ __forceinline__ void merged_step_lengths(cg_state* st, double delta, uint32_t* status) {
+    const double gamma = st->rr;
+    double beta = 0.0, denom = delta;
+    if (st->iter > 0) {
+        beta = gamma / st->rr_prev;
+        denom = delta - beta * gamma / st->alpha;
+    }
+    if (!(denom > 0.0) || !isfinite(denom)) {
+        record_status(status, kStatusBreakdown);
+        st->stop = 1u;
+        st->alpha = 0.0;
+        st->beta = 0.0;
+        return;
+    }
+    st->beta = beta;
+    st->alpha = gamma / denom;
+    st->dot = delta;
+}
 
 }  // namespace dimgpu

@@ -123,6 +123,9 @@ struct spmv_epilogue {
     const double* rr = nullptr;
     double* alpha_out = nullptr;
     uint32_t* halt = nullptr;        // when non-null and *halt != 0 on entry, the launch does nothing
+    // Merged CG engine: the last CTA computes alpha and beta of the Chronopoulos-Gear recurrence from
+    // dot = x.y and the state (merged_step_lengths, cg_common.cuh).
+    struct cg_state* merged = nullptr;
 };
 
 int launch_spmv_f64(const dimgpu_csr5* m, const double* x, double* y, dimgpu_calibrator* cal,
@@ -139,7 +142,10 @@ int autotune_f32(dimgpu_csr5* m, cudaStream_t stream);
 int vec_fill(uint64_t n, double v, double* y, cudaStream_t stream);
 
 // spmm.cu: CSR5 SpMM (lanes = right-hand sides, one pass takes k <= 32 columns)
-constexpr int kSpmmShapes = 2;  // launch shapes the autotuner chooses from (warps per CTA x stages)
+// SpMM shape codes the autotuner chooses from: bit 0 the launch shape (0: 8 warps x 3 stages, 1: 16 x 2),
+// bits 1-2 the lane grouping (0: the widest vector lanes the operands allow, 1: one right-hand side per
+// lane, 2: two per lane at k > 16)
+constexpr int kSpmmShapes = 6;
 struct spmm_args {
     const void* X = nullptr;
     void* Y = nullptr;
@@ -167,6 +173,7 @@ int spmm_scratch_init(spmm_scratch* s, const dimgpu_csr5* m);
 void spmm_scratch_release(spmm_scratch* s);
 int launch_spmm(const dimgpu_csr5* m, bool f32, const spmm_args& a, const spmm_scratch& sc, int shape,
                 cudaStream_t st);
+bool spmm_shape_applies(bool f32, const spmm_args& a, int shape);
 int autotune_spmm(const dimgpu_csr5* m, bool f32, const spmm_args& a, const spmm_scratch& sc, cudaStream_t st,
                   int* best_shape, float* best_ms);
 

@@ -730,26 +730,52 @@ int lanes_vec(const spmm_args& a, int kp) {
 // Lane-group width for k right-hand sides.
 inline int kp_for(uint32_t k) { return k <= 8 ? 8 : (k <= 16 ? 16 : 32); }
 
+// Right-hand sides per lane that a shape code's lane grouping (bits 1-2) selects for these operands:
+// 0 the widest vector lanes the operands allow, 1 one per lane, 2 two per lane (k rounded to 32 with
+// at least two-wide vector access).  -1 when the grouping does not apply (it would repeat another).
+template <typename VT>
+int lanes_for_shape(const spmm_args& a, int shape) {
+    const int grouping = shape >> 1;
+    if (sizeof(VT) == 8)
+        return grouping == 0 ? 1 : -1;  // FP64 is bound by the FP64 pipe: one value per lane
+    const int kp = kp_for(a.k);
+    const int widest = lanes_vec<VT>(a, kp);
+    switch (grouping) {
+    case 0:
+        return widest;
+    case 1:
+        return widest > 1 ? 1 : -1;
+    case 2:
+        return (kp == 32 && widest >= 4) ? 2 : -1;
+    default:
+        return -1;
+    }
+}
+
 template <typename VT, bool DOT>
 int mm_dispatch(const dimgpu_csr5* m, const VT* vals, const spmm_args& a, const spmm_scratch& sc, int shape,
                 cudaStream_t st) {
     const int kp = kp_for(a.k);
+    const int launch = shape & 1;
+    int v = lanes_for_shape<VT>(a, shape);
+    if (v < 0)
+        v = lanes_for_shape<VT>(a, launch);  // a grouping these operands cannot use: the default one
     if constexpr (sizeof(VT) == 4) {
-        // f32 is issue-bound: share the per-element work over four elements with vector lanes
-        const int v = lanes_vec<VT>(a, kp);
+        // f32 is issue-bound: vector lanes share the per-element work over two or four elements
         if (kp == 16 && v == 2)
-            return mm_dispatch_kp<VT, 16, 2, DOT>(m, vals, a, sc, shape, st);
+            return mm_dispatch_kp<VT, 16, 2, DOT>(m, vals, a, sc, launch, st);
         if (kp == 32 && v == 4)
-            return mm_dispatch_kp<VT, 32, 4, DOT>(m, vals, a, sc, shape, st);
+            return mm_dispatch_kp<VT, 32, 4, DOT>(m, vals, a, sc, launch, st);
+        if (kp == 32 && v == 2)
+            return mm_dispatch_kp<VT, 32, 2, DOT>(m, vals, a, sc, launch, st);
     }
-    // FP64 is bound by the FP64 pipe (the same DFMA count either way): one value per lane
     switch (kp) {
     case 8:
-        return mm_dispatch_kp<VT, 8, 1, DOT>(m, vals, a, sc, shape, st);
+        return mm_dispatch_kp<VT, 8, 1, DOT>(m, vals, a, sc, launch, st);
     case 16:
-        return mm_dispatch_kp<VT, 16, 1, DOT>(m, vals, a, sc, shape, st);
+        return mm_dispatch_kp<VT, 16, 1, DOT>(m, vals, a, sc, launch, st);
     default:
-        return mm_dispatch_kp<VT, 32, 1, DOT>(m, vals, a, sc, shape, st);
+        return mm_dispatch_kp<VT, 32, 1, DOT>(m, vals, a, sc, launch, st);
     }
 }
 
@@ -767,6 +793,8 @@ cudaError_t mm_attrs() {
         if ((e = mm_attr<VT, 16, 2, 16, 2, DOT>()) != cudaSuccess) return e;
         if ((e = mm_attr<VT, 32, 4, 8, 3, DOT>()) != cudaSuccess) return e;
         if ((e = mm_attr<VT, 32, 4, 16, 2, DOT>()) != cudaSuccess) return e;
+        if ((e = mm_attr<VT, 32, 2, 8, 3, DOT>()) != cudaSuccess) return e;
+        if ((e = mm_attr<VT, 32, 2, 16, 2, DOT>()) != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
@@ -837,8 +865,15 @@ int launch_spmm(const dimgpu_csr5* m, bool f32, const spmm_args& a, const spmm_s
                : mm_dispatch<double, false>(m, m->vals, a, sc, shape, st);
 }
 
-// Picks the launch shape (warps per CTA x pipeline stages) of one SpMM by timing each candidate on
-// the caller's operands.  Deterministic choice: the fastest of two timed launches per shape.
+bool spmm_shape_applies(bool f32, const spmm_args& a, int shape) {
+    if (shape < 0 || shape >= kSpmmShapes)
+        return false;
+    return f32 ? lanes_for_shape<float>(a, shape) > 0 : lanes_for_shape<double>(a, shape) > 0;
+}
+
+// Picks the shape of one SpMM -- launch shape (warps per CTA x pipeline stages) and lane grouping
+// (right-hand sides per lane) -- by timing each candidate that applies to the caller's operands.
+// Deterministic choice: the fastest of two timed launches per candidate.
 int autotune_spmm(const dimgpu_csr5* m, bool f32, const spmm_args& a, const spmm_scratch& sc, cudaStream_t st,
                   int* best_shape, float* best_ms) {
     cudaEvent_t e0, e1;
@@ -855,6 +890,8 @@ int autotune_spmm(const dimgpu_csr5* m, bool f32, const spmm_args& a, const spmm
     float bms = 1e30f;
     int rc = DIMGPU_OK;
     for (int shape = 0; shape < kSpmmShapes && rc == DIMGPU_OK; ++shape) {
+        if (!spmm_shape_applies(f32, plain, shape))
+            continue;
         if ((rc = launch_spmm(m, f32, plain, sc, shape, st)) != DIMGPU_OK)
             break;
         float ms_min = 1e30f;
@@ -943,5 +980,14 @@ extern "C" int dimgpu_csr5_spmm_shape(const dimgpu_csr5* m, uint32_t k, int f32,
     if (!m || !shape || k == 0 || k > 32)
         return dimgpu::fail(DIMGPU_ERR_INVALID_ARGUMENT, "bad argument");
     *shape = m->spmm_shape[f32 ? 1 : 0][k];
+    return DIMGPU_OK;
+}
+
+extern "C" int dimgpu_csr5_set_spmm_shape(dimgpu_csr5* m, uint32_t k, int f32, int shape) {
+    if (!m || k == 0 || k > 32)
+        return dimgpu::fail(DIMGPU_ERR_INVALID_ARGUMENT, "bad argument");
+    if (shape < -1 || shape >= dimgpu::kSpmmShapes)
+        return dimgpu::fail(DIMGPU_ERR_INVALID_ARGUMENT, "shape %d is not in [-1, %d)", shape, dimgpu::kSpmmShapes);
+    m->spmm_shape[f32 ? 1 : 0][k] = shape;
     return DIMGPU_OK;
 }

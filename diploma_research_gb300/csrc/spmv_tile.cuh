@@ -1,5 +1,4 @@
-// spmv_tile.cuh -- one CSR5 tile of the SpMV, shared by the standalone SpMV kernel (spmv.cu) and the
-// persistent CG kernel (cg_fused.cu).
+// spmv_tile.cuh -- one CSR5 tile of the SpMV kernel (spmv.cu).
 //
 // Reference: the per-tile part of csr5::spmv (include/dim/mat/storage_formats/csr5.h:640-745).
 // A warp processes one staged tile: lane c owns tile column c (sigma rows), gathers x, closes a

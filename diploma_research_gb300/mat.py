@@ -94,6 +94,23 @@ class csr:
         return csr(dimensions_t(a.shape[0], a.shape[1]), a.data, a.indptr.astype(np.uint32),
                    a.indices.astype(np.uint32))
 
+    def permuted(self, perm) -> "csr":
+        """P A P^T for a square matrix: new row/column i is old row/column perm[i] (columns re-sorted per
+        row).  CG on the permuted system, with b permuted the same way, gives the permuted solution."""
+        import scipy.sparse as sp
+
+        if self.dimensions.rows != self.dimensions.cols:
+            raise ValueError("a symmetric permutation needs a square matrix")
+        perm = np.asarray(perm, dtype=np.int64)
+        P = self.to_scipy()[perm][:, perm].tocsr()
+        P.sort_indices()
+        return csr.from_scipy(sp.csr_matrix(P))
+
+    def hub_first_order(self) -> np.ndarray:
+        """The permutation that numbers rows by decreasing length (stable): for a symmetric matrix the most
+        referenced columns then come first and their x entries share cache sectors."""
+        return np.argsort(-np.diff(self.row_start_offsets.astype(np.int64)), kind="stable")
+
     def iterate(self, body) -> None:
         """Calls ``body((row, col), value)`` for every stored element in row order (csr5.h:868-877)."""
         rp = self.row_start_offsets

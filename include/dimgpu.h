@@ -177,8 +177,14 @@ DIMGPU_API int dimgpu_csr5_spmm(const dimgpu_csr5* m, uint32_t k, const double* 
                                 uint64_t ldy, void* stream);
 DIMGPU_API int dimgpu_csr5_spmm_f32(const dimgpu_csr5* m, uint32_t k, const float* X, uint64_t ldx, float* Y,
                                     uint64_t ldy, void* stream);
-/* The launch shape the autotuner picked for (k, f32): 0 (8 warps x 3 stages) or 1 (16 x 2), -1 before the first call. */
+/* The shape the autotuner picked for (k, f32), -1 before the first call.  Bit 0 is the launch shape
+ * (0: 8 warps x 3 stages, 1: 16 x 2); bits 1-2 the lane grouping (0: the widest vector lanes the operands
+ * allow -- f32 lanes hold k/8 right-hand sides at k = 16, 32 --, 1: one right-hand side per lane, 2: two
+ * per lane at k > 16).  No reference counterpart (the reference has no SpMM). */
 DIMGPU_API int dimgpu_csr5_spmm_shape(const dimgpu_csr5* m, uint32_t k, int f32, int* shape);
+/* Pins the shape for (k, f32) (0..5; -1 re-tunes on the next call), e.g. for reproducible timings.  A
+ * grouping the operands cannot use falls back to grouping 0 with the same launch shape. */
+DIMGPU_API int dimgpu_csr5_set_spmm_shape(dimgpu_csr5* m, uint32_t k, int f32, int shape);
 
 /* ---- vectors (include/dim/vec.h:29-84), device memory ----------------------------------------- */
 
@@ -202,9 +208,12 @@ typedef struct {
     int32_t engine;    /* DIMGPU_CG_ENGINE_*: how a solve runs when use_graph != 0 */
 } dimgpu_cg_params;
 
-#define DIMGPU_CG_ENGINE_AUTO 0  /* the library's choice: currently the graph (faster on every measured system) */
-#define DIMGPU_CG_ENGINE_GRAPH 1 /* one CUDA graph per solve: 3 kernels per iteration in a device-side loop */
-#define DIMGPU_CG_ENGINE_FUSED 2 /* one persistent cooperative kernel per solve, grid barriers between phases */
+#define DIMGPU_CG_ENGINE_AUTO 0   /* the library's choice: currently the graph */
+#define DIMGPU_CG_ENGINE_GRAPH 1  /* one CUDA graph per solve, the reference's recurrence: 3 kernels per iteration
+                                     (SpMV + s.As, r update + r.r, x and s updates) in a device-side loop */
+#define DIMGPU_CG_ENGINE_MERGED 2 /* FP64 only: the same graph with the Chronopoulos-Gear recurrence (one reduction
+                                     phase per iteration): 2 kernels per iteration (SpMV + r.Ar, all vector
+                                     updates + r.r); the same iterates in exact arithmetic */
 
 typedef struct {
     int64_t iterations;      /* CG iterations (inner iterations for the mixed solver) */
@@ -268,7 +277,7 @@ DIMGPU_API int dimgpu_cg_adjoint(const dimgpu_csr5* m, const double* g, const do
 /* ---- diagnostics ------------------------------------------------------------------------------ */
 
 DIMGPU_API const char* dimgpu_last_error_string(void);
-/* ABI version of this library. */
+/* ABI version of this library (2: status queries, the merged CG engine in place of the persistent one). */
 DIMGPU_API int dimgpu_version(void);
 
 #ifdef __cplusplus

@@ -1,0 +1,217 @@
+// dimgpu.hpp -- C++ binding of the C ABI in dimgpu.h, shaped like the reference's interface.
+//
+// The reference ("dim") is used from C++ through the header-only template
+// dim::mat::csr5<double,16,4,uint32_t> (include/dim/mat/storage_formats/csr5.h:254-881) and the CG loop
+// of benchmarks/conjugate_gradient/dim_sp/main.cpp:78-141.  This header gives a C++ caller of dim the
+// same calls on the GPU library:
+//
+//   reference                                          here
+//   csr5::from_csr(csr) (csr5.h:791-803)               dim::gpu::csr5::from_csr(csr)
+//   csr5::spmv(spmv_data_t{x, y, calibrator})          csr5::spmv(x, y) on host spans,
+//     (csr5.h:280-285, 818-829)                          csr5::spmv_device(x, y, cal, stream) on device memory
+//   csr5::create_calibrator() (csr5.h:809)             csr5::create_calibrator()
+//   csr5::tail_partition_start(), non_zero_count()     the same names
+//   the dim_sp CG loop                                 dim::gpu::cg_solver
+//
+// from_csr takes any matrix type with the members of dim::mat::csr<double> (csr.h:19-40):
+// `dimensions.rows`, `dimensions.cols`, and contiguous `values`, `row_start_offsets` (u32) and
+// `col_indices` (u32) containers -- the reference's own csr<double> among them.
+//
+// Handles are move-only (a copy would free the device matrix twice).  Errors are exceptions, as in the
+// reference: a size mismatch or other bad argument throws std::invalid_argument (csr5.h:820-821), any
+// other failure dim::gpu::error carrying the library's status code.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <span>
+#include <stdexcept>
+#include <string>
+#include <utility>
+
+#include "dimgpu.h"
+
+namespace dim::gpu {
+
+class error : public std::runtime_error {
+public:
+    error(int code, const char* what) : std::runtime_error(what), code_(code) {}
+    int code() const noexcept { return code_; }
+
+private:
+    int code_;
+};
+
+[[noreturn]] inline void raise(int rc) {
+    const char* msg = dimgpu_last_error_string();
+    if (rc == DIMGPU_ERR_INVALID_ARGUMENT)
+        throw std::invalid_argument(msg);
+    throw error(rc, msg);
+}
+
+inline void check(int rc) {
+    if (rc != DIMGPU_OK)
+        raise(rc);
+}
+
+class csr5;
+
+// Scratch of one SpMV at a time (the reference's calibrator_t, csr5/calibrator.h:14-31).
+class calibrator {
+public:
+    calibrator() = default;
+    calibrator(const calibrator&) = delete;
+    calibrator& operator=(const calibrator&) = delete;
+    calibrator(calibrator&& o) noexcept : h_(std::exchange(o.h_, nullptr)) {}
+    calibrator& operator=(calibrator&& o) noexcept {
+        if (this != &o) {
+            reset();
+            h_ = std::exchange(o.h_, nullptr);
+        }
+        return *this;
+    }
+    ~calibrator() { reset(); }
+
+    dimgpu_calibrator* handle() const noexcept { return h_; }
+
+private:
+    friend class csr5;
+    explicit calibrator(dimgpu_calibrator* h) : h_(h) {}
+    void reset() noexcept {
+        if (h_)
+            dimgpu_calibrator_destroy(h_);
+        h_ = nullptr;
+    }
+    dimgpu_calibrator* h_{};
+};
+
+struct dimensions_t {
+    uint32_t rows{}, cols{};
+};
+
+// A CSR5 matrix in GPU memory.
+class csr5 {
+public:
+    csr5() = default;
+    csr5(const csr5&) = delete;
+    csr5& operator=(const csr5&) = delete;
+    csr5(csr5&& o) noexcept : h_(std::exchange(o.h_, nullptr)), info_(o.info_) {}
+    csr5& operator=(csr5&& o) noexcept {
+        if (this != &o) {
+            reset();
+            h_ = std::exchange(o.h_, nullptr);
+            info_ = o.info_;
+        }
+        return *this;
+    }
+    ~csr5() { reset(); }
+
+    // csr5::from_csr (csr5.h:791-803): conversion on the GPU from a host CSR matrix.  The reference
+    // takes the csr by value and moves it in; here the caller keeps it (the device holds copies).
+    template <typename Csr>
+    static csr5 from_csr(const Csr& m, const dimgpu_csr5_options* opt = nullptr, void* stream = nullptr) {
+        csr5 r;
+        const auto nnz = static_cast<uint64_t>(std::size(m.values));
+        if (std::size(m.col_indices) != nnz || std::size(m.row_start_offsets) != size_t(m.dimensions.rows) + 1)
+            throw std::invalid_argument("csr arrays do not match the matrix dimensions");
+        check(dimgpu_csr5_from_csr(static_cast<uint32_t>(m.dimensions.rows), static_cast<uint32_t>(m.dimensions.cols),
+                                   nnz, std::data(m.row_start_offsets), nnz ? std::data(m.col_indices) : nullptr,
+                                   nnz ? std::data(m.values) : nullptr, DIMGPU_MEM_HOST, opt, stream, &r.h_));
+        check(dimgpu_csr5_get_info(r.h_, &r.info_));
+        return r;
+    }
+
+    // y := A x on host spans (the reference's benchmark call with its spmv_data_t, csr5.h:818-829).
+    // Throws std::invalid_argument on a size mismatch, as the reference does (csr5.h:820-821).
+    void spmv(std::span<const double> x, std::span<double> y) const {
+        if (x.size() != info_.cols)
+            throw std::invalid_argument("can't multiply, vector size doesn't match column count of the matrix");
+        if (y.size() != info_.rows)
+            throw std::invalid_argument("output vector size doesn't match the row count of the matrix");
+        check(dimgpu_csr5_spmv_host(h_, x.data(), y.data()));
+    }
+
+    // y := A x on device memory, asynchronous on `stream`; cal == nullptr uses the matrix's own scratch.
+    // Device-side failures are reported by status(cal, stream).
+    void spmv_device(const double* x, double* y, const calibrator* cal = nullptr, void* stream = nullptr) const {
+        check(dimgpu_csr5_spmv(h_, x, y, cal ? cal->handle() : nullptr, stream));
+    }
+
+    // Synchronizes `stream` and throws dim::gpu::error when a product on this scratch recorded a failure.
+    void status(const calibrator* cal = nullptr, void* stream = nullptr) const {
+        check(dimgpu_csr5_status(h_, cal ? cal->handle() : nullptr, stream));
+    }
+
+    calibrator create_calibrator() const {
+        dimgpu_calibrator* c = nullptr;
+        check(dimgpu_calibrator_create(h_, &c));
+        return calibrator(c);
+    }
+
+    uint32_t tail_partition_start() const noexcept { return info_.tail_partition_start; }
+    size_t non_zero_count() const noexcept { return static_cast<size_t>(info_.nnz); }
+    dimensions_t dimensions() const noexcept { return {info_.rows, info_.cols}; }
+    const dimgpu_csr5_info& info() const noexcept { return info_; }
+    dimgpu_csr5* handle() const noexcept { return h_; }
+
+private:
+    void reset() noexcept {
+        if (h_)
+            dimgpu_csr5_destroy(h_);
+        h_ = nullptr;
+    }
+    dimgpu_csr5* h_{};
+    dimgpu_csr5_info info_{};
+};
+
+// The dim_sp CG loop (benchmarks/conjugate_gradient/dim_sp/main.cpp:89-127) on the GPU, stopping at
+// ||b - A x|| <= tol ||b|| (docs/paper/thesis.tex:2146-2148).  The matrix must outlive the solver.
+class cg_solver {
+public:
+    cg_solver(const csr5& a, const dimgpu_cg_params& params, void* stream = nullptr) : rows_(a.dimensions().rows) {
+        check(dimgpu_cg_create(a.handle(), &params, stream, &h_));
+    }
+    cg_solver(const cg_solver&) = delete;
+    cg_solver& operator=(const cg_solver&) = delete;
+    cg_solver(cg_solver&& o) noexcept : h_(std::exchange(o.h_, nullptr)), rows_(o.rows_) {}
+    cg_solver& operator=(cg_solver&& o) noexcept {
+        if (this != &o) {
+            reset();
+            h_ = std::exchange(o.h_, nullptr);
+            rows_ = o.rows_;
+        }
+        return *this;
+    }
+    ~cg_solver() { reset(); }
+
+    // Solves from the initial guess in x (host memory), overwriting it.  Returns the statistics; a solve
+    // that stops at max_it or breaks down throws dim::gpu::error (DIMGPU_ERR_NOT_CONVERGED / _BREAKDOWN)
+    // unless `throw_on_failure` is false, in which case stats.status tells.
+    dimgpu_cg_stats solve(std::span<const double> b, std::span<double> x, bool throw_on_failure = true) {
+        if (b.size() != rows_ || x.size() != rows_)
+            throw std::invalid_argument("b and x must have as many elements as the matrix has rows");
+        dimgpu_cg_stats st{};
+        const int rc = dimgpu_cg_solve_host(h_, b.data(), x.data(), &st);
+        if (rc != DIMGPU_OK && (throw_on_failure || (rc != DIMGPU_ERR_NOT_CONVERGED && rc != DIMGPU_ERR_BREAKDOWN)))
+            raise(rc);
+        return st;
+    }
+
+    // The same on device memory, on `stream`.
+    dimgpu_cg_stats solve_device(const double* b, double* x, void* stream = nullptr) {
+        dimgpu_cg_stats st{};
+        check(dimgpu_cg_solve(h_, b, x, &st, stream));
+        return st;
+    }
+
+private:
+    void reset() noexcept {
+        if (h_)
+            dimgpu_cg_destroy(h_);
+        h_ = nullptr;
+    }
+    dimgpu_cg_solver* h_{};
+    size_t rows_{};
+};
+
+}  // namespace dim::gpu

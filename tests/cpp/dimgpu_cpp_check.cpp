@@ -1,0 +1,132 @@
+// A C++ caller of dimgpu through include/dimgpu.hpp, as a dim user would write it: from_csr, spmv on
+// host spans and on device memory (CUDA runtime allocations, a stream, the status query), the CG
+// solver, and the reference's exceptions.
+//
+//   dimgpu_cpp_check <output file>
+//
+// Builds the 2-D 5-point Laplacian on a 64 x 64 grid, multiplies x_i = sin(0.37 i), solves A z = A x,
+// and writes n, x, y = A x and z (little-endian doubles after a u64 n) for the test to compare with the
+// oracle.  With DIMGPU_WITH_REFERENCE_CSR the matrix is the reference's own dim::mat::csr<double>
+// (include/dim/mat/storage_formats/csr.h); otherwise a struct with the same members stands in for it.
+#include <dimgpu.hpp>
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <type_traits>
+#include <vector>
+
+#ifdef DIMGPU_WITH_REFERENCE_CSR
+#include <dim/mat/storage_formats/csr.h>
+using csr_t = dim::mat::csr<double>;
+static csr_t make_csr(uint32_t n, const std::vector<double>& v, const std::vector<uint32_t>& rp,
+                      const std::vector<uint32_t>& ci) {
+    return csr_t{dim::mat::dimensions_t{.rows = n, .cols = n}, csr_t::values_t(v.begin(), v.end()),
+                 csr_t::indices_t(rp.begin(), rp.end()), csr_t::indices_t(ci.begin(), ci.end())};
+}
+#else
+struct csr_t {
+    struct {
+        uint32_t rows, cols;
+    } dimensions;
+    std::vector<double> values;
+    std::vector<uint32_t> row_start_offsets;
+    std::vector<uint32_t> col_indices;
+};
+static csr_t make_csr(uint32_t n, const std::vector<double>& v, const std::vector<uint32_t>& rp,
+                      const std::vector<uint32_t>& ci) {
+    return csr_t{{n, n}, v, rp, ci};
+}
+#endif
+
+static_assert(!std::is_copy_constructible_v<dim::gpu::csr5> && !std::is_copy_assignable_v<dim::gpu::csr5>);
+static_assert(std::is_nothrow_move_constructible_v<dim::gpu::csr5> && std::is_nothrow_move_assignable_v<dim::gpu::csr5>);
+static_assert(!std::is_copy_constructible_v<dim::gpu::calibrator> && !std::is_copy_constructible_v<dim::gpu::cg_solver>);
+
+#define EXPECT(c)                                                        \
+    do {                                                                 \
+        if (!(c)) {                                                      \
+            std::fprintf(stderr, "%s:%d: failed: %s\n", __FILE__, __LINE__, #c); \
+            return 1;                                                    \
+        }                                                                \
+    } while (0)
+
+int main(int argc, char** argv) {
+    if (argc < 2) {
+        std::fprintf(stderr, "usage: %s <output file>\n", argv[0]);
+        return 2;
+    }
+    const uint32_t g = 64, n = g * g;
+    std::vector<double> v;
+    std::vector<uint32_t> rp{0}, ci;
+    for (uint32_t i = 0; i < g; ++i)
+        for (uint32_t j = 0; j < g; ++j) {
+            const uint32_t r = i * g + j;
+            if (i > 0) ci.push_back(r - g), v.push_back(-1.0);
+            if (j > 0) ci.push_back(r - 1), v.push_back(-1.0);
+            ci.push_back(r), v.push_back(4.0);
+            if (j + 1 < g) ci.push_back(r + 1), v.push_back(-1.0);
+            if (i + 1 < g) ci.push_back(r + g), v.push_back(-1.0);
+            rp.push_back((uint32_t)ci.size());
+        }
+    const csr_t m = make_csr(n, v, rp, ci);
+
+    dim::gpu::csr5 tmp = dim::gpu::csr5::from_csr(m);
+    dim::gpu::csr5 A = std::move(tmp);  // move-only handle; tmp is empty now
+    EXPECT(tmp.handle() == nullptr && A.handle() != nullptr);
+    EXPECT(A.non_zero_count() == v.size() && A.dimensions().rows == n);
+
+    std::vector<double> x(n), y(n), z(n, 0.0);
+    for (uint32_t i = 0; i < n; ++i)
+        x[i] = std::sin(0.37 * i);
+    A.spmv(x, y);
+
+    // the reference's exception on a size mismatch (csr5.h:820-821)
+    bool threw = false;
+    try {
+        std::vector<double> short_x(n - 1);
+        A.spmv(short_x, y);
+    } catch (const std::invalid_argument&) {
+        threw = true;
+    }
+    EXPECT(threw);
+
+    // the same product on device memory with a calibrator, asynchronous on a stream
+    dim::gpu::calibrator cal = A.create_calibrator();
+    EXPECT(cal.handle() != nullptr);
+    double *dx = nullptr, *dy = nullptr;
+    EXPECT(cudaMalloc(&dx, n * sizeof(double)) == cudaSuccess && cudaMalloc(&dy, n * sizeof(double)) == cudaSuccess);
+    cudaStream_t s = nullptr;
+    EXPECT(cudaStreamCreate(&s) == cudaSuccess);
+    EXPECT(cudaMemcpyAsync(dx, x.data(), n * sizeof(double), cudaMemcpyHostToDevice, s) == cudaSuccess);
+    A.spmv_device(dx, dy, &cal, s);
+    A.status(&cal, s);  // synchronizes; throws if the product recorded a failure
+    std::vector<double> y_dev(n);
+    EXPECT(cudaMemcpy(y_dev.data(), dy, n * sizeof(double), cudaMemcpyDeviceToHost) == cudaSuccess);
+    EXPECT(y_dev == y);  // the same kernel on the same input: the same bits
+    cudaFree(dx);
+    cudaFree(dy);
+    cudaStreamDestroy(s);
+
+    dimgpu_cg_params p{};
+    p.tol = 1e-10;
+    p.max_it = 10000;
+    p.precision = DIMGPU_CG_FP64;
+    p.use_graph = 1;
+    dim::gpu::cg_solver solver(A, p);
+    const dimgpu_cg_stats st = solver.solve(y, z);
+    EXPECT(st.status == DIMGPU_OK && st.rel_residual <= 1.5e-10);
+    A.status();
+
+    FILE* f = std::fopen(argv[1], "wb");
+    EXPECT(f != nullptr);
+    const uint64_t nn = n;
+    std::fwrite(&nn, sizeof(nn), 1, f);
+    std::fwrite(x.data(), sizeof(double), n, f);
+    std::fwrite(y.data(), sizeof(double), n, f);
+    std::fwrite(z.data(), sizeof(double), n, f);
+    std::fclose(f);
+    std::printf("ok %lld iterations\n", (long long)st.iterations);
+    return 0;
+}

@@ -53,7 +53,7 @@ def test_argument_errors_without_device(native):
     assert native.dimgpu_csr5_spmv(None, None, None, None, None) == N.ERR_INVALID_ARGUMENT
     assert native.dimgpu_cg_create(None, None, None, None) == N.ERR_INVALID_ARGUMENT
     assert native.dimgpu_csr5_status(None, None, None) == N.ERR_INVALID_ARGUMENT
-    assert native.dimgpu_version() == 1
+    assert native.dimgpu_version() == 2
 
 
 def test_product_does_not_import_oracle():

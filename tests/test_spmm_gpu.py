@@ -2,19 +2,31 @@
 import numpy as np
 import pytest
 
-from diploma_research_gb300.csr5 import csr5, spmm, spmm_shape
+from diploma_research_gb300.csr5 import csr5, set_spmm_shape, spmm, spmm_shape
 from helpers import csr_from_lengths, random_csr
 
 pytestmark = pytest.mark.gpu
 
+U32 = 2.0 ** -24  # unit roundoff of f32
 
-def _check(torch, m, k, seed=0, f32=False):
+
+def _f32_bound(m, AX):
+    """Componentwise bound of an f32 product of rows of n elements: each of the n products and n - 1 sums
+    rounds once, so |y - y_exact| <= gamma_(n+1) (|A||X|) with gamma_j = j u / (1 - j u)."""
+    n = np.diff(m.row_start_offsets.astype(np.int64)).astype(np.float64)[:, None] + 1.0
+    return n * U32 / (1.0 - n * U32) * AX
+
+
+def _check(torch, m, k, seed=0, f32=False, A=None, shape=None):
     rng = np.random.default_rng(seed)
     X = rng.uniform(-1, 1, (m.dimensions.cols, k))
     S = m.to_scipy()
     Y_ref = S @ X
     AX = abs(S) @ np.abs(X)
-    A = csr5.from_csr(m)
+    if A is None:
+        A = csr5.from_csr(m)
+    if shape is not None:
+        set_spmm_shape(A, min(k, 32), shape, f32)
     dt = torch.float32 if f32 else torch.float64
     Xd = torch.tensor(X, device="cuda", dtype=dt)
     Yd = torch.full((m.dimensions.rows, k), float("nan"), device="cuda", dtype=dt)
@@ -22,11 +34,17 @@ def _check(torch, m, k, seed=0, f32=False):
     torch.cuda.synchronize()
     Y = Yd.cpu().numpy().astype(np.float64)
     if f32:
-        Y_ref = S @ X.astype(np.float32).astype(np.float64)
-    tol = 1e-4 if f32 else 1e-12
+        # the exact product of the f32-rounded operands (values and X), and the f32 rounding bound
+        S32 = S.copy()
+        S32.data = S32.data.astype(np.float32).astype(np.float64)
+        X32 = X.astype(np.float32).astype(np.float64)
+        Y_ref = S32 @ X32
+        bound = _f32_bound(m, abs(S32) @ np.abs(X32))
+    else:
+        bound = 1e-12 * AX
     err = np.abs(Y - Y_ref)
-    assert np.all(err <= tol * AX + 1e-300), float(np.max(err / (AX + 1e-300)))
-    assert spmm_shape(A, min(k, 32), f32) in (0, 1)
+    assert np.all(err <= bound + 1e-300), float(np.max(err / (bound + 1e-300)))
+    assert 0 <= spmm_shape(A, min(k, 32), f32) < 6
     return A
 
 
@@ -42,6 +60,18 @@ def test_spmm_f32(native, torch_cuda, k):
     rng = np.random.default_rng(100 + k)
     m = random_csr(rng, 3000, 3000, 9.0, empty_frac=0.05, long_rows=2, long_len=(600, 2000))
     _check(torch_cuda, m, k, seed=k, f32=True)
+
+
+@pytest.mark.parametrize("f32", [False, True])
+@pytest.mark.parametrize("k", [5, 8, 16, 24, 32])
+def test_spmm_every_shape(native, torch_cuda, k, f32):
+    """Every shape the autotuner may choose (launch shape x lane grouping), pinned, against the reference
+    product; groupings that do not apply to the operands fall back to grouping 0."""
+    rng = np.random.default_rng(200 + k)
+    m = random_csr(rng, 4000, 3500, 10.0, empty_frac=0.05, long_rows=3, long_len=(600, 3000))
+    A = csr5.from_csr(m)
+    for shape in range(6):
+        _check(torch_cuda, m, k, seed=shape, f32=f32, A=A, shape=shape)
 
 
 @pytest.mark.parametrize("lens,cols", [([3, 0, 5, 1], 10), ([0, 0, 0], 4), ([20000], 20000),
