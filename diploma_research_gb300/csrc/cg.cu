@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_update_merged64(const double
     }
     const uint64_t pol = policy_evict_last();
     double rr = 0;
-    constexpr int U = 2;  // five 16-byte loads per element: 40 registers of loaded data per round
+    constexpr int U = 1;  // five 16-byte loads per element: two rounds of them would spill at 64 registers
     double2 wv[U], zv[U], pv[U], xv[U], rv[U];
     vloop<U>(
         n / 2,
