@@ -69,13 +69,14 @@ def test_mm_mtx_device_layout(native):
     _dev_vs_oracle(m, 16)
 
 
+@pytest.mark.parametrize("sigma", [16, 32])
 @pytest.mark.parametrize("seed", range(10))
-def test_random_device_layout(native, seed):
+def test_random_device_layout(native, seed, sigma):
     rng = np.random.default_rng(seed)
     m = random_csr(rng, int(rng.integers(10, 6000)), int(rng.integers(10, 6000)), float(rng.uniform(0.2, 40)),
                    empty_frac=float(rng.choice([0, 0.1, 0.7])), long_rows=int(rng.integers(0, 5)),
                    long_len=(500, 3000))
-    _dev_vs_oracle(m, 16)
+    _dev_vs_oracle(m, sigma)
 
 
 @pytest.mark.parametrize("seed", range(4))
@@ -92,7 +93,9 @@ def test_edge_cases_device_layout(native):
     rng = np.random.default_rng(9)
     for lens, cols in [([3, 0, 5, 1], 10), ([0, 0, 0], 4), ([0] * 50 + [512] + [0] * 50, 600), ([5000], 6000),
                        ([0, 700, 0, 0, 2000, 1, 0], 3000), ([512] * 4, 512), ([1] * 2048, 7), ([0] * 1000 + [1], 2)]:
-        _dev_vs_oracle(csr_from_lengths(lens, cols, rng), 16)
+        m = csr_from_lengths(lens, cols, rng)
+        _dev_vs_oracle(m, 16)
+        _dev_vs_oracle(m, 32)
 
 
 def test_rejects_malformed_csr(native):
