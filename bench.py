@@ -218,7 +218,7 @@ def run_gpu(args):
     stream = torch.cuda.current_stream()
     bd = torch.tensor(b, device="cuda", dtype=torch.float64)
     xd = torch.zeros(n, device="cuda", dtype=torch.float64)
-    s64 = CGSolver(A, tol=TOL, precision="fp64", stream=stream, use_graph=not args.no_graph, engine=args.engine)
+    s64 = CGSolver(A, tol=TOL, precision="fp64", stream=stream, use_graph=not args.no_graph)
     smx = CGSolver(A, tol=TOL, precision="mixed", stream=stream, use_graph=not args.no_graph)
 
     def solve(solver):
@@ -501,7 +501,7 @@ def run_batch(args):
 
     B.build()
     from diploma_research_gb300.cg import BlockCGSolver, CGSolver
-    from diploma_research_gb300.csr5 import csr5, spmm_shape
+    from diploma_research_gb300.csr5 import csr5
     from diploma_research_gb300.generators import WORKLOADS, rhs
 
     m = WORKLOADS["lap3d7_192"]["build"]()
@@ -527,7 +527,7 @@ def run_batch(args):
             out[prec] = {"seconds": sec, "rhs_solves_per_s": k / sec, "iterations": res.iterations,
                          "converged_columns": res.converged_columns, "max_rel_residual": res.max_rel_residual,
                          "reliable_updates": res.reliable_updates, "rel_error_vs_xstar": err}
-            out[prec]["spmm_shape"] = spmm_shape(A, min(k, 32), prec == "mixed")
+            out[prec]["spmm_shape"] = res.spmm_shape
             del s
         sep = []
         for j in range(k):
@@ -672,8 +672,6 @@ def main():
                     help="with --spmv-only: time the f64 and f32 SpMV in every launch configuration")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven CG loop instead of the CUDA graph (profilers list every kernel)")
-    ap.add_argument("--engine", default="auto", choices=["auto", "graph", "merged"],
-                    help="CG engine of the FP64 solve (the mixed solve always runs the graph engine)")
     ap.add_argument("--batch", default=None, help="comma-separated k: the multi-RHS block-CG workload")
     ap.add_argument("--adjoint", action="store_true", help="the differentiable-solve workload (adjoint CG)")
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(DESCR),

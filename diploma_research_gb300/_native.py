@@ -54,7 +54,7 @@ class cg_params(ctypes.Structure):
                 ("use_graph", ctypes.c_int32), ("reliable_delta", ctypes.c_double), ("engine", ctypes.c_int32)]
 
 
-CG_ENGINE_AUTO, CG_ENGINE_GRAPH, CG_ENGINE_MERGED = 0, 1, 2
+CG_ENGINE_AUTO, CG_ENGINE_GRAPH = 0, 1
 
 
 class cg_stats(ctypes.Structure):
@@ -66,7 +66,8 @@ class cg_stats(ctypes.Structure):
 class block_cg_stats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int64), ("reliable_updates", ctypes.c_int64),
                 ("max_rel_residual", ctypes.c_double), ("seconds", ctypes.c_double),
-                ("converged_columns", ctypes.c_int32), ("status", ctypes.c_int32)]
+                ("converged_columns", ctypes.c_int32), ("status", ctypes.c_int32), ("spmm_shape", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class DimgpuError(RuntimeError):

@@ -29,13 +29,12 @@ class cg_result:
 
 
 _PREC = {"fp64": N.CG_FP64, "mixed": N.CG_MIXED}
-_ENGINE = {"auto": N.CG_ENGINE_AUTO, "graph": N.CG_ENGINE_GRAPH, "merged": N.CG_ENGINE_MERGED}
+_ENGINE = {"auto": N.CG_ENGINE_AUTO, "graph": N.CG_ENGINE_GRAPH}
 
 
 class CGSolver:
-    """engine: "auto" (the library's choice, currently the graph), "graph" (one CUDA graph, three kernels
-    per iteration, the reference's recurrence) or "merged" (FP64 only: the Chronopoulos-Gear recurrence,
-    two kernels per iteration); use_graph=False runs the same kernels from a host-driven loop."""
+    """engine: "auto" or "graph" (one CUDA graph, three kernels per iteration, the reference's
+    recurrence); use_graph=False runs the same kernels from a host-driven loop."""
 
     def __init__(self, A: csr5, tol: float = 1e-10, max_it: int = 100000, precision: str = "fp64",
                  use_graph: bool = True, reliable_delta: float = 0.03, stream=None, engine: str = "auto"):
@@ -96,7 +95,7 @@ class block_cg_result:
     converged_columns: int
     col_iterations: list
     col_rel_residual: list
-
+    spmm_shape: int = -1           # the autotuned shape of the iteration's SpMM
 
 class BlockCGSolver:
     """k <= 32 simultaneous CG solves sharing one CSR5 SpMM per iteration, per-column convergence masks.
@@ -134,7 +133,7 @@ class BlockCGSolver:
         rc = N.lib().dimgpu_block_cg_solve(self._h, N.device_ptr(B, "<f8"), self.k, N.device_ptr(X, "<f8"), self.k,
                                            ctypes.byref(st), its, rel, N.stream_ptr(stream))
         res = block_cg_result(int(st.iterations), int(st.reliable_updates), float(st.max_rel_residual),
-                              float(st.seconds), int(st.converged_columns), list(its), list(rel))
+                              float(st.seconds), int(st.converged_columns), list(its), list(rel), int(st.spmm_shape))
         if rc != N.OK and (raise_on_failure or rc not in (N.ERR_NOT_CONVERGED, N.ERR_BREAKDOWN)):
             N.check(rc)
         return X, res

@@ -847,6 +847,8 @@ int dimgpu_block_cg_solve(dimgpu_block_cg* s, const double* B, uint64_t ldb, dou
         stats->seconds = ms * 1e-3;
         stats->converged_columns = (int32_t)nconv;
         stats->status = status;
+        stats->spmm_shape = bmixed(s) ? s->shape32 : s->shape64;
+        stats->reserved = 0;
     }
     if (status == DIMGPU_ERR_NOT_CONVERGED)
         set_error("block CG: %u of %u columns converged within max_it", nconv, s->k);

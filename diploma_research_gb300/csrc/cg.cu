@@ -12,14 +12,6 @@
 // The whole solve is one CUDA graph: init kernels, then a conditional WHILE node whose body is four
 // iterations; kernel B sets the loop condition from the device, so the solve makes no host round trip.
 //
-// The merged engine (FP64) runs the same solve with the Chronopoulos-Gear recurrence, which needs one
-// reduction phase per iteration instead of two and so two kernels instead of three:
-//   M1  SpMV w = A r fused with delta = r.w; its last CTA computes beta = gamma / gamma_prev and
-//       alpha = gamma / (delta - beta gamma / alpha_prev) (merged_step_lengths, cg_common.cuh)
-//   M2  z = w + beta z (z = A p), p = r + beta p, x += alpha p, r -= alpha z, gamma = r.r; its last block
-//       decides convergence on gamma like kernel B
-// In exact arithmetic its iterates are the reference loop's; in floating point they differ by rounding.
-//
 // Mixed precision runs the same recurrence on f32 values and f32 vectors s, As, r.  Products and short
 // partial sums are f32, every dot product is accumulated in f64, alpha and beta are f64, and the
 // iterate is kept as x (f64) + y (f32 correction since the last flush).  Whenever r.r has dropped by
@@ -294,116 +286,6 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_update_xs64(double* x, doubl
 }
 
 // ---------------------------------------------------------------------------------------------
-// merged (Chronopoulos-Gear) f64 solver
-// ---------------------------------------------------------------------------------------------
-
-// r = b - Ax; p = 0; z = 0; gamma = r.r; bb = b.b
-__global__ void __launch_bounds__(kVecThreads, 2) k_init_merged64(const double* b, const double* Ax, double* r,
-                                                               double* p, double* z, uint64_t n, vec_ctx c) {
-    const uint64_t pol = policy_evict_last();
-    double rr = 0, bb = 0;
-    constexpr int U = 1;  // runs once per solve
-    double2 bv[U], av[U];
-    vloop<U>(
-        n / 2,
-        [&](uint64_t i, int u) {
-            bv[u] = ld2_keep(b + 2 * i, pol);
-            av[u] = ld2_keep(Ax + 2 * i, pol);
-        },
-        [&](uint64_t i, int u) {
-            const double2 bi = bv[u], ai = av[u];
-            const double2 ri = make_double2(bi.x - ai.x, bi.y - ai.y);
-            st2_stream(r + 2 * i, ri, pol);
-            st2_stream(p + 2 * i, make_double2(0.0, 0.0), pol);
-            st2_stream(z + 2 * i, make_double2(0.0, 0.0), pol);
-            rr = fma(ri.x, ri.x, fma(ri.y, ri.y, rr));
-            bb = fma(bi.x, bi.x, fma(bi.y, bi.y, bb));
-        });
-    vtail(n, 2, [&](uint64_t i) {
-        const double ri = b[i] - Ax[i];
-        r[i] = ri;
-        p[i] = 0.0;
-        z[i] = 0.0;
-        rr = fma(ri, ri, rr);
-        bb = fma(b[i], b[i], bb);
-    });
-    double trr, tbb;
-    if (grid_reduce2(rr, bb, c, &trr, &tbb)) {
-        cg_state* st = c.st;
-        st->rr = trr;
-        st->rr_prev = trr;
-        st->bb = tbb;
-        st->thresh2 = st->thresh2 * (tbb > 0 ? tbb : 1.0);  // holds tol^2 on entry
-        st->iter = 0;
-        st->x_pending = 0;
-        st->converged = trr <= st->thresh2 ? 1u : 0u;
-        st->stop = st->converged || st->max_it <= 0;
-        set_loop(c, !st->stop);
-    }
-}
-
-// z = w + beta z; p = r + beta p; x += alpha p; r -= alpha z; gamma' = r.r; decide
-__global__ void __launch_bounds__(kVecThreads, 2) k_update_merged64(const double* w, double* z, double* p, double* x,
-                                                                 double* r, uint64_t n, vec_ctx c) {
-    cg_state* st = c.st;
-    const uint32_t stop = st->stop;
-    const double alpha = st->alpha, beta = st->beta;
-    if (stop) {
-        if (blockIdx.x == 0 && threadIdx.x == 0)
-            set_loop(c, false);
-        return;
-    }
-    const uint64_t pol = policy_evict_last();
-    double rr = 0;
-    constexpr int U = 1;  // five 16-byte loads per element: two rounds of them would spill at 64 registers
-    double2 wv[U], zv[U], pv[U], xv[U], rv[U];
-    vloop<U>(
-        n / 2,
-        [&](uint64_t i, int u) {
-            wv[u] = ld2_keep(w + 2 * i, pol);
-            zv[u] = ld2_keep(z + 2 * i, pol);
-            pv[u] = ld2_keep(p + 2 * i, pol);
-            xv[u] = ld2_keep(x + 2 * i, pol);
-            rv[u] = ld2_keep(r + 2 * i, pol);
-        },
-        [&](uint64_t i, int u) {
-            const double2 wi = wv[u], zo = zv[u], po = pv[u], xo = xv[u], ro = rv[u];
-            const double2 zi = make_double2(fma(beta, zo.x, wi.x), fma(beta, zo.y, wi.y));
-            const double2 pi = make_double2(fma(beta, po.x, ro.x), fma(beta, po.y, ro.y));
-            const double2 ri = make_double2(fma(-alpha, zi.x, ro.x), fma(-alpha, zi.y, ro.y));
-            st2_stream(z + 2 * i, zi, pol);
-            st2_stream(p + 2 * i, pi, pol);
-            st2_stream(x + 2 * i, make_double2(fma(alpha, pi.x, xo.x), fma(alpha, pi.y, xo.y)), pol);
-            st2_stream(r + 2 * i, ri, pol);
-            rr = fma(ri.x, ri.x, fma(ri.y, ri.y, rr));
-        });
-    vtail(n, 2, [&](uint64_t i) {
-        const double zi = fma(beta, z[i], w[i]);
-        const double pi = fma(beta, p[i], r[i]);
-        const double ri = fma(-alpha, zi, r[i]);
-        z[i] = zi;
-        p[i] = pi;
-        x[i] = fma(alpha, pi, x[i]);
-        r[i] = ri;
-        rr = fma(ri, ri, rr);
-    });
-    double t, unused;
-    if (grid_reduce2(rr, 0.0, c, &t, &unused)) {
-        st->rr_prev = st->rr;
-        st->rr = t;
-        st->rr_new = t;
-        st->iter += 1;
-        if (t <= st->thresh2) {
-            st->converged = 1;
-            st->stop = 1;
-        } else if (st->iter >= st->max_it || !isfinite(t)) {
-            st->stop = 1;
-        }
-        set_loop(c, !st->stop);
-    }
-}
-
-// ---------------------------------------------------------------------------------------------
 // mixed solver
 // ---------------------------------------------------------------------------------------------
 
@@ -648,8 +530,8 @@ struct dimgpu_cg_solver {
     dimgpu_cg_params params{};
     int grid = 1;
     uint64_t n = 0;
-    // f64 vectors (merged engine: s holds p, As holds w = A r, z = A p)
-    double *b = nullptr, *x = nullptr, *r = nullptr, *s = nullptr, *As = nullptr, *Ax = nullptr, *z = nullptr;
+    // f64 vectors
+    double *b = nullptr, *x = nullptr, *r = nullptr, *s = nullptr, *As = nullptr, *Ax = nullptr;
     // f32 vectors (mixed)
     float *r32 = nullptr, *s32 = nullptr, *As32 = nullptr, *y32 = nullptr;
     cg_state* st = nullptr;
@@ -657,7 +539,6 @@ struct dimgpu_cg_solver {
     uint32_t* counter = nullptr;
     double* norms = nullptr;
     dimgpu_calibrator cal{};  // SpMV scratch of this solver (f32 and f64 products take turns)
-    int merged = 0;           // the Chronopoulos-Gear recurrence (DIMGPU_CG_ENGINE_MERGED)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -677,9 +558,9 @@ void solver_free(dimgpu_cg_solver* s) {
     if (s->ev1)
         cudaEventDestroy(s->ev1);
     calibrator_release(&s->cal);
-    for (void* p : {(void*)s->b, (void*)s->x, (void*)s->r, (void*)s->s, (void*)s->As, (void*)s->Ax, (void*)s->z,
-                    (void*)s->r32, (void*)s->s32, (void*)s->As32, (void*)s->y32, (void*)s->st, (void*)s->part,
-                    (void*)s->counter, (void*)s->norms})
+    for (void* p : {(void*)s->b, (void*)s->x, (void*)s->r, (void*)s->s, (void*)s->As, (void*)s->Ax, (void*)s->r32,
+                    (void*)s->s32, (void*)s->As32, (void*)s->y32, (void*)s->st, (void*)s->part, (void*)s->counter,
+                    (void*)s->norms})
         dev_free(p);
     delete s;
 }
@@ -694,15 +575,10 @@ vec_ctx make_ctx(dimgpu_cg_solver* s) {
 
 bool mixed(const dimgpu_cg_solver* s) { return s->params.precision == DIMGPU_CG_MIXED; }
 
-// The engine DIMGPU_CG_ENGINE_AUTO takes: the three-kernel graph (the reference's recurrence).
-bool auto_merged(int /*precision*/) { return false; }
-
 // Enqueues the init kernels (needs s->x and s->b filled).
 int enqueue_init(dimgpu_cg_solver* s, const vec_ctx& c, cudaStream_t st) {
     DG_CHECK(launch_spmv_f64(s->m, s->x, s->Ax, &s->cal, spmv_epilogue{}, st));
-    if (s->merged)
-        k_init_merged64<<<s->grid, kVecThreads, 0, st>>>(s->b, s->Ax, s->r, s->s, s->z, s->n, c);
-    else if (mixed(s))
+    if (mixed(s))
         k_init_mixed<<<s->grid, kVecThreads, 0, st>>>(s->b, s->Ax, s->r32, s->s32, s->y32, s->n, c);
     else
         k_init64<<<s->grid, kVecThreads, 0, st>>>(s->b, s->Ax, s->r, s->s, s->n, c);
@@ -734,13 +610,7 @@ int enqueue_reliable_update(dimgpu_cg_solver* s, const vec_ctx& c, cudaStream_t 
 
 // One whole iteration as a plain stream of kernels (host-driven loop).
 int enqueue_iteration(dimgpu_cg_solver* s, const vec_ctx& c, cudaStream_t st) {
-    if (s->merged) {
-        spmv_epilogue ep;
-        ep.merged = s->st;
-        ep.halt = &s->st->stop;
-        DG_CHECK(launch_spmv_f64(s->m, s->r, s->As, &s->cal, ep, st));
-        k_update_merged64<<<s->grid, kVecThreads, 0, st>>>(s->As, s->z, s->s, s->x, s->r, s->n, c);
-    } else if (mixed(s)) {
+    if (mixed(s)) {
         DG_CHECK(launch_spmv_f32(s->m, s->s32, s->As32, &s->cal, cg_epilogue(s), st));
         k_update_r_mixed<<<s->grid, kVecThreads, 0, st>>>(s->As32, s->r32, s->s32, s->y32, s->n, c);
         k_update_s_mixed<<<s->grid, kVecThreads, 0, st>>>(s->s32, s->r32, s->n, s->st, 0);
@@ -825,7 +695,7 @@ int build_graph(dimgpu_cg_solver* s) {
         cudaGraph_t body;
         if ((rc = add_conditional(g, leaves, c.loop, cudaGraphCondTypeWhile, &wnode, &body)) != DIMGPU_OK)
             break;
-        if (!mixed(s) || s->merged) {
+        if (!mixed(s)) {
             rc = capture_into(cap, body, {}, nullptr, [&]() -> int {
                 for (int u = 0; u < kGraphUnroll; ++u)
                     DG_CHECK(enqueue_iteration(s, c, cap));
@@ -902,11 +772,8 @@ int dimgpu_cg_create(const dimgpu_csr5* m, const dimgpu_cg_params* params, void*
         return fail(DIMGPU_ERR_INVALID_ARGUMENT, "unknown precision %d", params->precision);
     if (m->layout != kLayoutDevice)
         return fail(DIMGPU_ERR_UNSUPPORTED, "CG needs a device-layout matrix");
-    if (params->engine != DIMGPU_CG_ENGINE_AUTO && params->engine != DIMGPU_CG_ENGINE_GRAPH &&
-        params->engine != DIMGPU_CG_ENGINE_MERGED)
+    if (params->engine != DIMGPU_CG_ENGINE_AUTO && params->engine != DIMGPU_CG_ENGINE_GRAPH)
         return fail(DIMGPU_ERR_INVALID_ARGUMENT, "unknown engine %d", params->engine);
-    if (params->engine == DIMGPU_CG_ENGINE_MERGED && params->precision != DIMGPU_CG_FP64)
-        return fail(DIMGPU_ERR_UNSUPPORTED, "the merged engine runs the FP64 solver only");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     dimgpu_cg_solver* s = new dimgpu_cg_solver();
     s->m = m;
@@ -914,8 +781,6 @@ int dimgpu_cg_create(const dimgpu_csr5* m, const dimgpu_cg_params* params, void*
     if (s->params.reliable_delta <= 0 || s->params.reliable_delta >= 1)
         s->params.reliable_delta = 0.03;
     s->n = m->rows;
-    s->merged = params->engine == DIMGPU_CG_ENGINE_MERGED ||
-                (params->engine == DIMGPU_CG_ENGINE_AUTO && auto_merged(params->precision));
     const int sms = device_sm_count(m->device);
     // two resident blocks per SM (fewer for short vectors)
     s->grid = (int)std::max<uint64_t>(
@@ -936,7 +801,6 @@ int dimgpu_cg_create(const dimgpu_csr5* m, const dimgpu_cg_params* params, void*
             if ((rc = dev_alloc_n(&s->r, n)) != DIMGPU_OK) break;
             if ((rc = dev_alloc_n(&s->s, n)) != DIMGPU_OK) break;
             if ((rc = dev_alloc_n(&s->As, n)) != DIMGPU_OK) break;
-            if (s->merged && (rc = dev_alloc_n(&s->z, n)) != DIMGPU_OK) break;
         }
         if ((rc = dev_alloc_n(&s->st, 1)) != DIMGPU_OK) break;
         if ((rc = dev_alloc_n(&s->part, 2 * (uint64_t)s->grid)) != DIMGPU_OK) break;

@@ -124,9 +124,6 @@ struct spmv_epilogue {
     const double* rr = nullptr;
     double* alpha_out = nullptr;
     uint32_t* halt = nullptr;        // when non-null and *halt != 0 on entry, the launch does nothing
-    // Merged CG engine: the last CTA computes alpha and beta of the Chronopoulos-Gear recurrence from
-    // dot = x.y and the state (merged_step_lengths, cg_common.cuh).
-    struct cg_state* merged = nullptr;
 };
 
 int launch_spmv_f64(const dimgpu_csr5* m, const double* x, double* y, dimgpu_calibrator* cal,

@@ -42,7 +42,6 @@
 #include <mutex>
 #include <vector>
 
-#include "cg_common.cuh"
 #include "common.cuh"
 #include "internal.hpp"
 #include "layout.cuh"
@@ -88,7 +87,6 @@ struct spmv_params {
     const double* rr;
     double* alpha_out;
     uint32_t* halt;
-    cg_state* merged;
 #ifdef DIMGPU_TEST_HOOKS
     uint32_t withhold_run;  // test builds only: this run never publishes its flag word (0xffffffff = none)
 #endif
@@ -311,8 +309,6 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
                 dot += s_red[wi];
             if (p.dot_out)
                 *p.dot_out = dot;
-            if (p.merged)
-                merged_step_lengths(p.merged, dot, p.status);
             if (p.rr) {
                 if (!(dot > 0.0) || !isfinite(dot)) {
                     record_status(p.status, kStatusBreakdown);
@@ -377,7 +373,6 @@ int launch_cfg(const dimgpu_csr5* m, const VT* vals, const VT* x, VT* y, dimgpu_
     p.rr = ep.rr;
     p.alpha_out = ep.alpha_out;
     p.halt = ep.halt;
-    p.merged = ep.merged;
 #ifdef DIMGPU_TEST_HOOKS
     p.withhold_run = g_test_withhold_run;
 #endif
@@ -514,7 +509,7 @@ int launch_spmv_f64(const dimgpu_csr5* m, const double* x, double* y, dimgpu_cal
                     const spmv_epilogue& ep, cudaStream_t stream) {
     if (m->layout != kLayoutDevice || m->omega != 32)
         return fail(DIMGPU_ERR_UNSUPPORTED, "SpMV needs the 32-lane device layout");
-    const bool dot = ep.dot_out || ep.alpha_out || ep.merged;
+    const bool dot = ep.dot_out || ep.alpha_out;
     switch (m->sigma) {
     case 16:
         if (m->plan.warps_per_cta == kWPCL1)
@@ -538,7 +533,7 @@ int launch_spmv_f32(const dimgpu_csr5* m, const float* x, float* y, dimgpu_calib
     if (m->layout != kLayoutDevice || m->omega != 32)
         return fail(DIMGPU_ERR_UNSUPPORTED, "SpMV needs the 32-lane device layout");
     DG_CHECK(ensure_vals32(m, stream));
-    const bool dot = ep.dot_out || ep.alpha_out || ep.merged;
+    const bool dot = ep.dot_out || ep.alpha_out;
     switch (m->sigma) {
     case 16:
         if (m->plan32.warps_per_cta == kWPC32L1)

@@ -205,15 +205,12 @@ typedef struct {
     int32_t precision; /* DIMGPU_CG_FP64 or DIMGPU_CG_MIXED */
     int32_t use_graph; /* 0: host-driven loop of kernels; otherwise the engine below */
     double reliable_delta; /* mixed only: replace the residual when it dropped by this factor; 0 = 0.03 (CG), 0.1 (block CG) */
-    int32_t engine;    /* DIMGPU_CG_ENGINE_*: how a solve runs when use_graph != 0 */
+    int32_t engine;    /* DIMGPU_CG_ENGINE_AUTO or _GRAPH: how a solve runs when use_graph != 0 */
 } dimgpu_cg_params;
 
-#define DIMGPU_CG_ENGINE_AUTO 0   /* the library's choice: currently the graph */
+#define DIMGPU_CG_ENGINE_AUTO 0   /* the library's choice: the graph */
 #define DIMGPU_CG_ENGINE_GRAPH 1  /* one CUDA graph per solve, the reference's recurrence: 3 kernels per iteration
                                      (SpMV + s.As, r update + r.r, x and s updates) in a device-side loop */
-#define DIMGPU_CG_ENGINE_MERGED 2 /* FP64 only: the same graph with the Chronopoulos-Gear recurrence (one reduction
-                                     phase per iteration): 2 kernels per iteration (SpMV + r.Ar, all vector
-                                     updates + r.r); the same iterates in exact arithmetic */
 
 typedef struct {
     int64_t iterations;      /* CG iterations (inner iterations for the mixed solver) */
@@ -243,11 +240,14 @@ typedef struct {
     double seconds;           /* device time of the solve */
     int32_t converged_columns;
     int32_t status;           /* DIMGPU_OK, _NOT_CONVERGED or _BREAKDOWN */
+    int32_t spmm_shape;       /* the autotuned shape of the iteration's SpMM (f32 for MIXED), as dimgpu_csr5_spmm_shape */
+    int32_t reserved;
 } dimgpu_block_cg_stats;
 
 /* k simultaneous CG solves (the dim_sp recurrence per column, its own alpha_j/beta_j) sharing one
  * CSR5 SpMM per iteration; a column stops when it converges (per-column mask).  params as for
- * dimgpu_cg_create (precision FP64 or MIXED).  Autotunes the SpMM launch shape on creation. */
+ * dimgpu_cg_create (precision FP64 or MIXED; engine AUTO or GRAPH).  Autotunes the SpMM shape (launch
+ * shape and lane grouping) on its own blocks on creation. */
 DIMGPU_API int dimgpu_block_cg_create(const dimgpu_csr5* m, uint32_t k, const dimgpu_cg_params* params,
                                       void* stream, dimgpu_block_cg** out);
 DIMGPU_API int dimgpu_block_cg_destroy(dimgpu_block_cg* s);
@@ -277,7 +277,7 @@ DIMGPU_API int dimgpu_cg_adjoint(const dimgpu_csr5* m, const double* g, const do
 /* ---- diagnostics ------------------------------------------------------------------------------ */
 
 DIMGPU_API const char* dimgpu_last_error_string(void);
-/* ABI version of this library (2: status queries, the merged CG engine in place of the persistent one). */
+/* ABI version of this library (2: status queries, SpMM shapes with lane grouping, no persistent CG engine). */
 DIMGPU_API int dimgpu_version(void);
 
 #ifdef __cplusplus

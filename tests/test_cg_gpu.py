@@ -36,7 +36,7 @@ def test_reference_fixture_cg(native):
 
 
 # (engine, use_graph): use_graph=False runs the same kernels from a host-driven loop
-ENGINES = [("graph", True), ("merged", True), ("graph", False), ("merged", False)]
+ENGINES = [("graph", True), ("graph", False)]
 
 
 @pytest.mark.parametrize("engine,use_graph", ENGINES)
@@ -62,35 +62,24 @@ def test_graph_and_host_loop_agree_bitwise(native):
     assert np.array_equal(x1, x2)
 
 
-def test_merged_is_reproducible_and_agrees_with_graph(native):
-    """The merged engine (Chronopoulos-Gear recurrence) sums in a fixed order: bitwise repeatable, and
-    within rounding of the reference's recurrence (the graph engine)."""
+def test_graph_is_reproducible(native):
+    """Fixed-order reductions: two solves give the same bits, FP64 and mixed."""
     m = laplacian_2d_5pt(80)
     _, b = rhs(m, 5)
     A = csr5.from_csr(m)
-    x1, r1 = cg(A, b, tol=1e-10, engine="merged")
-    x2, r2 = cg(A, b, tol=1e-10, engine="merged")
-    assert r1.iterations == r2.iterations and np.array_equal(x1, x2)
-    x3, r3 = cg(A, b, tol=1e-10, engine="graph")
-    assert r1.converged and r3.converged
-    assert abs(r1.iterations - r3.iterations) <= 2
-    assert np.linalg.norm(x1 - x3) / np.linalg.norm(x3) < 1e-8
+    for prec in ("fp64", "mixed"):
+        x1, r1 = cg(A, b, tol=1e-10, precision=prec)
+        x2, r2 = cg(A, b, tol=1e-10, precision=prec)
+        assert r1.iterations == r2.iterations and np.array_equal(x1, x2)
 
 
-def test_merged_graph_and_host_loop_agree_bitwise(native):
-    m = laplacian_2d_5pt(48)
-    _, b = rhs(m, 1)
-    A = csr5.from_csr(m)
-    x1, r1 = cg(A, b, tol=1e-9, use_graph=True, engine="merged")
-    x2, r2 = cg(A, b, tol=1e-9, use_graph=False, engine="merged")
-    assert r1.iterations == r2.iterations
-    assert np.array_equal(x1, x2)
-
-
-def test_merged_engine_is_fp64_only(native):
+def test_retired_engine_value_is_rejected(native):
     A = csr5.from_csr(laplacian_2d_5pt(16))
-    with pytest.raises(N.DimgpuError):
-        CGSolver(A, precision="mixed", engine="merged")
+    import ctypes
+
+    p = N.cg_params(1e-10, 100, N.CG_FP64, 1, 0.03, 2)  # 2 named the persistent engine, since removed
+    h = ctypes.c_void_p()
+    assert N.lib().dimgpu_cg_create(A._h, ctypes.byref(p), None, ctypes.byref(h)) == N.ERR_INVALID_ARGUMENT
 
 
 @pytest.mark.parametrize("n,density,long_rows,long_len,empty", [
@@ -100,34 +89,38 @@ def test_merged_engine_is_fp64_only(native):
     (60000, 12.0, 20, (2000, 9000), 0.05),  # many long rows
 ])
 def test_initial_residual_on_general_matrices(native, n, density, long_rows, long_len, empty):
-    """With max_it = 0 a solve stops after r0 = b - A x0, whose norm it reports: the SpMV inside each
-    engine on general matrices (look-back over warp runs, CSR tail, empty rows)."""
+    """With max_it = 0 a solve stops after r0 = b - A x0, whose norm it reports: the SpMV inside the
+    solver on general matrices (look-back over warp runs, CSR tail, empty rows)."""
     rng = np.random.default_rng(n)
     m = random_csr(rng, n, n, density, empty_frac=empty, long_rows=long_rows, long_len=long_len)
     A = csr5.from_csr(m)
     x0 = rng.uniform(-1, 1, n)
     b = rng.uniform(-1, 1, n)
     ref = np.linalg.norm(b - m.to_scipy() @ x0)
-    for engine, prec in (("graph", "fp64"), ("graph", "mixed"), ("merged", "fp64")):
-        _, res = CGSolver(A, tol=0.0, max_it=0, engine=engine, precision=prec).solve(b, x0, raise_on_failure=False)
+    for prec in ("fp64", "mixed"):
+        _, res = CGSolver(A, tol=0.0, max_it=0, precision=prec).solve(b, x0, raise_on_failure=False)
         got = res.recurrence_rel_residual * np.linalg.norm(b)
-        assert abs(got - ref) <= 1e-12 * ref, (engine, prec, got, ref)
+        assert abs(got - ref) <= 1e-12 * ref, (prec, got, ref)
 
 
-@pytest.mark.parametrize("engine,precision", [("graph", "fp64"), ("graph", "mixed"), ("merged", "fp64")])
-def test_power_law_cg(native, engine, precision):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_power_law_cg(native, precision):
+    """A power-law system whose CG iteration count moves with the summation order: the reference's loop
+    takes 282 iterations with 16 OpenMP threads and 285 with 8 (the calibrator chunks differ), a scipy CG
+    285, and shuffling the order of every row's sum alone gives 283-287.  Bar: 3 % of the oracle's
+    count, and the solution against the oracle's."""
     m = power_law(30000, 2.0, 3000, 7)
     xs, b = rhs(m, 7)
     A = csr5.from_csr(m)
-    x, res = cg(A, b, tol=1e-10, engine=engine, precision=precision)
+    x, res = cg(A, b, tol=1e-10, precision=precision)
     assert res.converged and res.rel_residual <= 1e-10 * 1.01
     xo, ito, _ = _oracle_cg(m, b, 1e-10)
     if precision == "fp64":
-        assert abs(res.iterations - ito) <= 2
+        assert abs(res.iterations - ito) <= max(2, int(np.ceil(0.03 * ito))), (res.iterations, ito)
     assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-7
 
 
-@pytest.mark.parametrize("engine", ["graph", "merged"])
+@pytest.mark.parametrize("engine", ["auto", "graph"])
 def test_device_buffers_and_nonzero_x0(native, torch_cuda, engine):
     m = laplacian_2d_5pt(40)
     xs, b = rhs(m, 2)
@@ -157,7 +150,7 @@ def test_mixed_precision_reaches_fp64_residual(native):
     assert res.iterations <= 2 * ito
 
 
-@pytest.mark.parametrize("engine", ["graph", "merged"])
+@pytest.mark.parametrize("engine", ["auto", "graph"])
 def test_not_converged_and_breakdown(native, engine):
     m = laplacian_2d_5pt(64)
     _, b = rhs(m, 4)
@@ -175,7 +168,7 @@ def test_not_converged_and_breakdown(native, engine):
     assert res.converged
 
 
-@pytest.mark.parametrize("engine", ["graph", "merged"])
+@pytest.mark.parametrize("engine", ["auto", "graph"])
 def test_zero_rhs(native, engine):
     m = laplacian_2d_5pt(16)
     A = csr5.from_csr(m)
@@ -184,12 +177,12 @@ def test_zero_rhs(native, engine):
 
 
 @pytest.mark.slow
-@pytest.mark.parametrize("engine,precision", [("graph", "fp64"), ("merged", "fp64"), ("graph", "mixed")])
-def test_stencil27_128_cg(native, precision, engine):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_stencil27_128_cg(native, precision):
     m = stencil_3d_27pt(128)
     xs, b = rhs(m, 1)
     A = csr5.from_csr(m)
-    x, res = cg(A, b, tol=1e-10, precision=precision, engine=engine)
+    x, res = cg(A, b, tol=1e-10, precision=precision)
     assert res.converged and res.rel_residual <= 1e-10 * 1.01
     if precision == "fp64":
         xo, ito, _ = _oracle_cg(m, b, 1e-10)  # the reference's CG loop on the same system

@@ -320,8 +320,8 @@ def test_sigma32_edge_cases(native, torch_cuda, lens, cols):
 
 @pytest.mark.parametrize("warps,gather", [(10, "l1"), (10, "stream"), (8, "l1"), (8, "stream")])
 def test_every_sigma32_launch_configuration(native, torch_cuda, warps, gather):
-    """Each f64 launch at sigma = 32, pinned: the product, the product with the fused dot, a CG solve in
-    both engines against the oracle's CG."""
+    """Each f64 launch at sigma = 32, pinned: the product, the product with the fused dot, and an FP64 CG
+    solve against the oracle's CG."""
     from diploma_research_gb300 import _native as N
     from diploma_research_gb300.cg import cg
 
@@ -351,10 +351,9 @@ def test_every_sigma32_launch_configuration(native, torch_cuda, warps, gather):
                         rng.uniform(-1, 1, L.dimensions.rows))
     o = oracle.OracleCSR5(L.dimensions.rows, L.dimensions.cols, L.row_start_offsets, L.col_indices, L.values)
     xo, ito, _ = o.cg(b, tol=1e-10)
-    for engine in ("graph", "merged"):
-        x, res = cg(A, b, tol=1e-10, engine=engine)
-        assert res.converged and res.rel_residual <= 1e-10 and abs(res.iterations - ito) <= 2
-        assert np.linalg.norm(x - xo) <= 1e-8 * np.linalg.norm(xo)
+    x, res = cg(A, b, tol=1e-10)
+    assert res.converged and res.rel_residual <= 1e-10 and abs(res.iterations - ito) <= 2
+    assert np.linalg.norm(x - xo) <= 1e-8 * np.linalg.norm(xo)
 
 
 def test_sigma32_has_no_f32_product(native, torch_cuda):
