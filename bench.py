@@ -434,7 +434,7 @@ def _time_all_launches(A, n):
     y = torch.empty(n, device="cuda", dtype=torch.float64)
     x32, y32 = x.float(), torch.empty(n, device="cuda", dtype=torch.float32)
     out = {"chosen_f64": A.spmv_launch(False)}
-    configs = [(False, (16, 12)), (True, (24, 20))] if A.sigma == 16 else [(False, (10, 8))]
+    configs = [(False, (16, 12)), (True, (24, 20))] if A.sigma == 16 else [(False, (9, 8))]
     if A.sigma == 16:
         out["chosen_f32"] = A.spmv_launch(True)
     for f32, wpcs in configs:

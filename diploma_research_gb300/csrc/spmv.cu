@@ -394,12 +394,17 @@ constexpr int kWPC32 = 24;    // f32: 24 warps x 2 stages x 4.2 KB per SM
 constexpr int kWPC32L1 = 20;  // f32, L1-leaning: 20 warps, 168 KB of stages
 // f64 at sigma = 32 (1024-element tiles, 10.3 KB stages with 16-bit column offsets): 35 FP64
 // instructions per lane and 1024 elements instead of 2 x 19 at sigma = 16, for the FP64-bound product
-constexpr int kWPCS32 = 10;    // 10 warps x 2 stages: 210 KB
-constexpr int kWPCS32L1 = 8;   // 8 warps: 168 KB, more L1
+constexpr int kWPCS32 = 9;     // 9 warps x 2 stages: 185 KB (221 KB with 32-bit indices)
+constexpr int kWPCS32L1 = 8;   // 8 warps: 164 KB (196 KB), more L1
 constexpr int kStages = 2;
+
+// Dynamic shared memory a CTA may use on sm_103a (227 KB), less room for the kernel's static arrays.
+constexpr size_t kMaxDynSmem = 232448 - 1024;
 
 template <typename VT, int SIGMA, int WPC, int STAGES, bool DOT>
 cudaError_t set_smem_attr() {
+    static_assert(smem_bytes<VT, SIGMA, WPC, STAGES, false>() <= kMaxDynSmem, "stages exceed shared memory");
+    static_assert(smem_bytes<VT, SIGMA, WPC, STAGES, true>() <= kMaxDynSmem, "stages exceed shared memory");
     cudaError_t e;
     const int bytes = (int)smem_bytes<VT, SIGMA, WPC, STAGES, false>();
     if ((e = cudaFuncSetAttribute(k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXReadOnly, false>,
@@ -605,7 +610,7 @@ int time_configs(dimgpu_csr5* m, int nconf, Set set, cudaStream_t stream, int* c
 int default_spmv_warps(uint32_t sigma) { return sigma == 32 ? kWPCS32 : kWPC; }
 
 // Chooses the f64 SpMV's launch for this matrix by timing: warps per CTA (16, or 12 to leave more L1;
-// 10 or 8 at sigma = 32) times how the x gathers load (kept in L1, or streamed past it).  Small
+// 9 or 8 at sigma = 32) times how the x gathers load (kept in L1, or streamed past it).  Small
 // matrices keep the default.
 int autotune_gathers(dimgpu_csr5* m, cudaStream_t stream) {
     m->x_mode = kXReadOnly;

@@ -318,7 +318,7 @@ def test_sigma32_edge_cases(native, torch_cuda, lens, cols):
     _check(torch_cuda, m, rng.uniform(-1, 1, cols), sigma=32)
 
 
-@pytest.mark.parametrize("warps,gather", [(10, "l1"), (10, "stream"), (8, "l1"), (8, "stream")])
+@pytest.mark.parametrize("warps,gather", [(9, "l1"), (9, "stream"), (8, "l1"), (8, "stream")])
 def test_every_sigma32_launch_configuration(native, torch_cuda, warps, gather):
     """Each f64 launch at sigma = 32, pinned: the product, the product with the fused dot, and an FP64 CG
     solve against the oracle's CG."""
