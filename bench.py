@@ -399,7 +399,7 @@ def run_spmv_only(args):
     if args.layout == "hub_first":
         m = m.permuted(m.hub_first_order())
     n, nnz = m.dimensions.rows, m.nnz
-    A = csr5.from_csr(m, sigma=args.sigma)
+    A = csr5.from_csr(m)
     if args.all_launches:
         return _time_all_launches(A, n)
     stream = torch.cuda.current_stream()
@@ -433,11 +433,8 @@ def _time_all_launches(A, n):
     x = torch.tensor(np.random.default_rng(5).uniform(-1, 1, n), device="cuda", dtype=torch.float64)
     y = torch.empty(n, device="cuda", dtype=torch.float64)
     x32, y32 = x.float(), torch.empty(n, device="cuda", dtype=torch.float32)
-    out = {"chosen_f64": A.spmv_launch(False)}
-    configs = [(False, (16, 12)), (True, (24, 20))] if A.sigma == 16 else [(False, (9, 8))]
-    if A.sigma == 16:
-        out["chosen_f32"] = A.spmv_launch(True)
-    for f32, wpcs in configs:
+    out = {"chosen_f64": A.spmv_launch(False), "chosen_f32": A.spmv_launch(True)}
+    for f32, wpcs in ((False, (16, 12)), (True, (24, 20))):
         xx, yy = (x32, y32) if f32 else (x, y)
         for w in wpcs:
             for g in ("l1", "stream"):
@@ -666,8 +663,6 @@ def main():
     ap.add_argument("--f32", action="store_true", help="with --spmv-only / --spmm-only: the f32 product")
     ap.add_argument("--layout", default="as_generated", choices=["as_generated", "hub_first"],
                     help="with --spmv-only: the matrix as generated or renumbered by decreasing row length")
-    ap.add_argument("--sigma", type=int, default=16, choices=[16, 32],
-                    help="with --spmv-only: rows per tile column of the device layout (32: f64 product only)")
     ap.add_argument("--all-launches", action="store_true",
                     help="with --spmv-only: time the f64 and f32 SpMV in every launch configuration")
     ap.add_argument("--no-graph", action="store_true",

@@ -248,9 +248,9 @@ int dimgpu_csr5_from_csr(uint32_t rows, uint32_t cols, uint64_t nnz, const uint3
         }
         if ((rc = prepare_spmv_kernels()) != DIMGPU_OK) break;
         if ((rc = convert_csr5(m, d_rp, d_ci, d_v, s)) != DIMGPU_OK) break;
-        const bool kernel_sigma = m->layout == kLayoutDevice && (m->sigma == 16 || m->sigma == 32);
+        const bool kernel_sigma = m->layout == kLayoutDevice && m->sigma == 16;
         if (kernel_sigma && (rc = build_col16(m, s)) != DIMGPU_OK) break;
-        m->plan = make_spmv_plan(m->tile_count, device_sm_count(m->device), default_spmv_warps(m->sigma));
+        m->plan = make_spmv_plan(m->tile_count, device_sm_count(m->device), 16);
         {
             // A matrix that fits in L2 together with the CG vectors (six f64 n-vectors) is better left
             // there between products than streamed with an evict-first policy.

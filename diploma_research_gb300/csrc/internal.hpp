@@ -110,7 +110,6 @@ int build_col16(dimgpu_csr5* m, cudaStream_t stream);
 
 // spmv.cu
 spmv_plan make_spmv_plan(uint64_t tiles, int sms, int warps_per_cta);
-int default_spmv_warps(uint32_t sigma);  // f64 SpMV warps per CTA before tuning
 spmv_plan make_spmv_plan32(uint64_t tiles, int sms);
 int prepare_spmv_kernels();
 int calibrator_init(dimgpu_calibrator* c, const dimgpu_csr5* m);

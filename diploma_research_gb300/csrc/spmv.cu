@@ -392,10 +392,6 @@ constexpr int kWPC = 16;      // f64: 16 warps x 2 stages x 6.3 KB per SM (regis
 constexpr int kWPCL1 = 12;    // f64, L1-leaning: 12 warps, 151 KB of stages
 constexpr int kWPC32 = 24;    // f32: 24 warps x 2 stages x 4.2 KB per SM
 constexpr int kWPC32L1 = 20;  // f32, L1-leaning: 20 warps, 168 KB of stages
-// f64 at sigma = 32 (1024-element tiles, 10.3 KB stages with 16-bit column offsets): 35 FP64
-// instructions per lane and 1024 elements instead of 2 x 19 at sigma = 16, for the FP64-bound product
-constexpr int kWPCS32 = 9;     // 9 warps x 2 stages: 185 KB (221 KB with 32-bit indices)
-constexpr int kWPCS32L1 = 8;   // 8 warps: 164 KB (196 KB), more L1
 constexpr int kStages = 2;
 
 // Dynamic shared memory a CTA may use on sm_103a (227 KB), less room for the kernel's static arrays.
@@ -437,10 +433,6 @@ int prepare_spmv_kernels() {
     DG_CUDA((set_smem_attr<float, 16, kWPC32, kStages, true>()));
     DG_CUDA((set_smem_attr<float, 16, kWPC32L1, kStages, false>()));
     DG_CUDA((set_smem_attr<float, 16, kWPC32L1, kStages, true>()));
-    DG_CUDA((set_smem_attr<double, 32, kWPCS32, kStages, false>()));
-    DG_CUDA((set_smem_attr<double, 32, kWPCS32, kStages, true>()));
-    DG_CUDA((set_smem_attr<double, 32, kWPCS32L1, kStages, false>()));
-    DG_CUDA((set_smem_attr<double, 32, kWPCS32L1, kStages, true>()));
     done = 1;
     return DIMGPU_OK;
 }
@@ -476,7 +468,7 @@ int calibrator_init(dimgpu_calibrator* c, const dimgpu_csr5* m) {
     // slots for every launch configuration the matrix may use, so that pinning another keeps it valid
     const int sms = device_sm_count(m->device);
     uint32_t most = std::max(m->plan.nwarps, m->plan32.nwarps);
-    for (int w : {kWPC, kWPCL1, kWPC32, kWPC32L1, kWPCS32, kWPCS32L1})
+    for (int w : {kWPC, kWPCL1, kWPC32, kWPC32L1})
         most = std::max(most, make_spmv_plan(m->tile_count, sms, w).nwarps);
     c->nslots = std::max<uint32_t>(most, 1);
     DG_CHECK(dev_alloc_n(&c->cal_val, c->nslots));
@@ -522,12 +514,6 @@ int launch_spmv_f64(const dimgpu_csr5* m, const double* x, double* y, dimgpu_cal
                        : launch_idx<double, 16, kWPCL1, kStages, false>(m, m->vals, x, y, cal, ep, stream);
         return dot ? launch_idx<double, 16, kWPC, kStages, true>(m, m->vals, x, y, cal, ep, stream)
                    : launch_idx<double, 16, kWPC, kStages, false>(m, m->vals, x, y, cal, ep, stream);
-    case 32:
-        if (m->plan.warps_per_cta == kWPCS32L1)
-            return dot ? launch_idx<double, 32, kWPCS32L1, kStages, true>(m, m->vals, x, y, cal, ep, stream)
-                       : launch_idx<double, 32, kWPCS32L1, kStages, false>(m, m->vals, x, y, cal, ep, stream);
-        return dot ? launch_idx<double, 32, kWPCS32, kStages, true>(m, m->vals, x, y, cal, ep, stream)
-                   : launch_idx<double, 32, kWPCS32, kStages, false>(m, m->vals, x, y, cal, ep, stream);
     default:
         return fail(DIMGPU_ERR_UNSUPPORTED, "sigma %u has no SpMV kernel", m->sigma);
     }
@@ -607,17 +593,14 @@ int time_configs(dimgpu_csr5* m, int nconf, Set set, cudaStream_t stream, int* c
     return rc;
 }
 
-int default_spmv_warps(uint32_t sigma) { return sigma == 32 ? kWPCS32 : kWPC; }
-
-// Chooses the f64 SpMV's launch for this matrix by timing: warps per CTA (16, or 12 to leave more L1;
-// 9 or 8 at sigma = 32) times how the x gathers load (kept in L1, or streamed past it).  Small
-// matrices keep the default.
+// Chooses the f64 SpMV's launch for this matrix by timing: warps per CTA (16, or 12 to leave more L1)
+// times how the x gathers load (kept in L1, or streamed past it).  Small matrices keep the default.
 int autotune_gathers(dimgpu_csr5* m, cudaStream_t stream) {
     m->x_mode = kXReadOnly;
-    if (m->tile_count < (m->sigma == 32 ? 2048u : 4096u) || m->rows == 0 || m->cols == 0)
+    if (m->tile_count < 4096 || m->rows == 0 || m->cols == 0)
         return DIMGPU_OK;
     const int sms = device_sm_count(m->device);
-    const int wpc[2] = {m->sigma == 32 ? kWPCS32 : kWPC, m->sigma == 32 ? kWPCS32L1 : kWPCL1};
+    const int wpc[2] = {kWPC, kWPCL1};
     const int mode[2] = {kXReadOnly, kXStream};
     auto set = [&](int i) {
         m->plan = make_spmv_plan(m->tile_count, sms, wpc[i / 2]);
@@ -812,16 +795,15 @@ extern "C" int dimgpu_csr5_set_spmv_launch(dimgpu_csr5* m, int f32, uint32_t war
     using namespace dimgpu;
     if (!m)
         return fail(DIMGPU_ERR_INVALID_ARGUMENT, "NULL matrix");
-    if (m->layout != kLayoutDevice || (m->sigma != 16 && m->sigma != 32) || (f32 && m->sigma != 16))
-        return fail(DIMGPU_ERR_UNSUPPORTED,
-                    "the SpMV launch is chosen for the 32-lane device layout at sigma 16 (f64 also at sigma 32)");
+    if (m->layout != kLayoutDevice || m->sigma != 16)
+        return fail(DIMGPU_ERR_UNSUPPORTED, "the SpMV launch is chosen only for the 32-lane device layout at sigma 16");
     if (gather != DIMGPU_GATHER_L1 && gather != DIMGPU_GATHER_STREAM)
         return fail(DIMGPU_ERR_INVALID_ARGUMENT, "gather mode %d", gather);
-    const int wa = f32 ? kWPC32 : (m->sigma == 32 ? kWPCS32 : kWPC);
-    const int wb = f32 ? kWPC32L1 : (m->sigma == 32 ? kWPCS32L1 : kWPCL1);
+    const int wa = f32 ? kWPC32 : kWPC;
+    const int wb = f32 ? kWPC32L1 : kWPCL1;
     if (warps_per_cta != (uint32_t)wa && warps_per_cta != (uint32_t)wb)
-        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "%u warps per CTA is not an %s SpMV launch at sigma %u (%d or %d)",
-                    warps_per_cta, f32 ? "f32" : "f64", m->sigma, wa, wb);
+        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "%u warps per CTA is not an %s SpMV launch (%d or %d)",
+                    warps_per_cta, f32 ? "f32" : "f64", wa, wb);
     const spmv_plan pl = make_spmv_plan(m->tile_count, device_sm_count(m->device), (int)warps_per_cta);
     const int mode = gather == DIMGPU_GATHER_STREAM ? kXStream : kXReadOnly;
     if (f32) {

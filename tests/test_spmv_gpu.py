@@ -299,74 +299,6 @@ def test_every_f32_launch_configuration(native, torch_cuda, warps, gather):
     assert res.converged and res.rel_residual <= 1e-10
 
 
-@pytest.mark.parametrize("seed", range(8))
-def test_sigma32_f64(native, torch_cuda, seed):
-    """The f64 product on the 1024-element tiles of sigma = 32 (64-bit descriptor words), on random
-    matrices with empty rows and long rows."""
-    rng = np.random.default_rng(300 + seed)
-    m = random_csr(rng, int(rng.integers(1, 9000)), int(rng.integers(1, 9000)), float(rng.uniform(0.1, 60)),
-                   empty_frac=float(rng.choice([0, 0.05, 0.5, 0.9])), long_rows=int(rng.integers(0, 6)),
-                   long_len=(100, 6000))
-    _check(torch_cuda, m, rng.uniform(-1, 1, m.dimensions.cols), sigma=32)
-
-
-@pytest.mark.parametrize("lens,cols", [([3, 0, 5, 1], 10), ([0] * 50 + [1024] + [0] * 50, 1200), ([40000], 40000),
-                                       ([1] * 5000, 3), ([0, 2000, 0, 0, 5000, 1, 0], 6000), ([31, 33] * 600, 900)])
-def test_sigma32_edge_cases(native, torch_cuda, lens, cols):
-    rng = np.random.default_rng(len(lens))
-    m = csr_from_lengths(lens, cols, rng)
-    _check(torch_cuda, m, rng.uniform(-1, 1, cols), sigma=32)
-
-
-@pytest.mark.parametrize("warps,gather", [(9, "l1"), (9, "stream"), (8, "l1"), (8, "stream")])
-def test_every_sigma32_launch_configuration(native, torch_cuda, warps, gather):
-    """Each f64 launch at sigma = 32, pinned: the product, the product with the fused dot, and an FP64 CG
-    solve against the oracle's CG."""
-    from diploma_research_gb300 import _native as N
-    from diploma_research_gb300.cg import cg
-
-    torch = torch_cuda
-    rng = np.random.default_rng(170 + warps)
-    for m in _launch_matrices(rng):
-        n = m.dimensions.rows
-        A = csr5.from_csr(m, sigma=32)
-        A.set_spmv_launch(warps, gather)
-        assert A.spmv_launch() == (warps, gather)
-        x = rng.uniform(-1, 1, n)
-        xd = torch.tensor(x, device="cuda", dtype=torch.float64)
-        yd = torch.full((n,), float("nan"), device="cuda", dtype=torch.float64)
-        dot = torch.zeros(1, device="cuda", dtype=torch.float64)
-        N.check(native.dimgpu_csr5_spmv_dot(A._h, xd.data_ptr(), yd.data_ptr(), dot.data_ptr(), None, None))
-        torch.cuda.synchronize()
-        y_ref, ax = _refs(m, x)
-        assert_spmv_close(yd.cpu().numpy(), y_ref, ax, SPMV_RTOL_F64)
-        assert abs(float(dot.item()) - float(np.dot(x, y_ref))) <= 1e-12 * float(np.dot(np.abs(x), ax))
-        assert_spmv_close(_gpu_spmv(torch, A, x), y_ref, ax, SPMV_RTOL_F64)
-    from diploma_research_gb300.generators import laplacian_2d_5pt
-
-    L = laplacian_2d_5pt(64)
-    A = csr5.from_csr(L, sigma=32)
-    A.set_spmv_launch(warps, gather)
-    b = oracle.csr_spmv(L.dimensions.rows, L.row_start_offsets, L.col_indices, L.values,
-                        rng.uniform(-1, 1, L.dimensions.rows))
-    o = oracle.OracleCSR5(L.dimensions.rows, L.dimensions.cols, L.row_start_offsets, L.col_indices, L.values)
-    xo, ito, _ = o.cg(b, tol=1e-10)
-    x, res = cg(A, b, tol=1e-10)
-    assert res.converged and res.rel_residual <= 1e-10 and abs(res.iterations - ito) <= 2
-    assert np.linalg.norm(x - xo) <= 1e-8 * np.linalg.norm(xo)
-
-
-def test_sigma32_has_no_f32_product(native, torch_cuda):
-    """At sigma = 32 only the f64 product (and the FP64 solvers) run; the f32 product refuses cleanly."""
-    torch = torch_cuda
-    from diploma_research_gb300 import _native as N
-
-    A = csr5.from_csr(random_csr(np.random.default_rng(4), 3000, 3000, 9.0), sigma=32)
-    x = torch.zeros(3000, device="cuda", dtype=torch.float32)
-    with pytest.raises(N.DimgpuError):
-        A.spmv(x, torch.zeros(3000, device="cuda", dtype=torch.float32))
-
-
 def test_launch_configuration_errors(native, torch_cuda):
     A = csr5.from_csr(random_csr(np.random.default_rng(1), 500, 500, 5.0))
     with pytest.raises(ValueError):
