@@ -201,8 +201,8 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
                 failed = true;
                 break;
             }
-            process_tile<VT, SIGMA, DOT, XM, IDX16, WPC>(io, ring + (size_t)s * G::STAGE, lane, t, raw, raw_n, pol_keep,
-                                                         ch, base);
+            process_tile<VT, SIGMA, DOT, XM, IDX16>(io, ring + (size_t)s * G::STAGE, lane, t, raw, raw_n, pol_keep, ch,
+                                                    base);
 
             __syncwarp();
             if (lane == 0 && t + STAGES < t_end) {

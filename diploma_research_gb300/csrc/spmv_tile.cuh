@@ -106,10 +106,9 @@ __device__ __forceinline__ void load_column(const unsigned char* stage, unsigned
     }
 }
 
-// x gathers in flight ahead of their products per lane (see process_tile): all of a column's, except in
-// the 20-warp FP64 launch, whose 96-register budget holds 8.
-template <typename VT, int SIGMA, int WPC>
-constexpr int kGatherAhead = (sizeof(VT) == 8 && WPC >= 20 && SIGMA > 8) ? 8 : SIGMA;
+// x gathers in flight ahead of their products per lane (see process_tile).
+template <typename VT, int SIGMA>
+constexpr int kGatherAhead = sizeof(VT) == 8 ? (SIGMA < 8 ? SIGMA : 8) : SIGMA;
 
 // The carry chain of one warp over its run of tiles (values uniform across the lanes).
 template <typename VT>
@@ -163,7 +162,7 @@ __device__ __forceinline__ void chain_write_row(const tile_io<VT>& io, warp_chai
 // Processes tile t staged at `st` (its values, column indices and descriptor words).  raw / raw_next are
 // tile_ptr[t] and tile_ptr[t + 1] with their dirty bits.  The stage's value area is reused as the
 // staging buffer of the tile's closed rows; the caller must __syncwarp() before refilling the stage.
-template <typename VT, int SIGMA, bool DOT, int XM = kXReadOnly, bool IDX16 = false, int WPC = 16>
+template <typename VT, int SIGMA, bool DOT, int XM = kXReadOnly, bool IDX16 = false>
 __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned char* st, unsigned lane, uint64_t t,
                                              uint32_t raw, uint32_t raw_next, uint64_t pol_keep, warp_chain<VT>& ch,
                                              uint32_t col_base = 0) {
@@ -177,10 +176,10 @@ __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned cha
     column_index<SIGMA, IDX16> ci;
     load_column<VT, SIGMA, IDX16>(st, lane, col_base, v, ci);
     const Word w = sd[lane];
-    // x gathers run AHEAD rows ahead of the products that use them.  Normally all of them are issued at
-    // once; the 20-warp FP64 launch, whose warps wait on the FP64 pipe between products anyway, keeps 8 in
-    // flight and so fewer registers, which is what lets 20 warps share an SM.
-    constexpr int AHEAD = kGatherAhead<VT, SIGMA, WPC>;
+    // x gathers run AHEAD rows ahead of the products that use them: the f32 product (latency-bound) issues
+    // all of them at once; the FP64 product, whose warps wait on the FP64 pipe between products, keeps
+    // fewer in flight and so fewer registers, which lets more warps share an SM.
+    constexpr int AHEAD = kGatherAhead<VT, SIGMA>;
     VT xv[SIGMA];
 #pragma unroll
     for (int r = 0; r < AHEAD; ++r)

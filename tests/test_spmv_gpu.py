@@ -244,9 +244,7 @@ def test_every_f64_launch_configuration(native, torch_cuda, warps, gather):
     for m in _launch_matrices(rng):
         n = m.dimensions.rows
         A = csr5.from_csr(m)
-        T = A.tile_count
-        base = 12 * m.nnz + 4 * (n + 1) + 8 * (T + 1) + 4 * T * 32
-        if warps == 20 and A.device_bytes - base < 2 * T * 512:
+        if warps == 20 and A.device_bytes < 12 * m.nnz + 2 * A.tile_count * 512:
             with pytest.raises(ValueError):  # no 16-bit column offsets: the 20-warp launch does not exist
                 A.set_spmv_launch(warps, gather)
             continue
