@@ -390,9 +390,6 @@ int launch_cfg(const dimgpu_csr5* m, const VT* vals, const VT* x, VT* y, dimgpu_
 // per precision, timed at conversion (f64) and when its f32 values are made (f32).
 constexpr int kWPC = 16;      // f64: 16 warps x 2 stages x 6.3 KB per SM (register-limited)
 constexpr int kWPCL1 = 12;    // f64, L1-leaning: 12 warps, 151 KB of stages
-// f64 with 16-bit column offsets only: 20 warps x 2 stages x 5.1 KB = 210 KB (96 registers per thread, so
-// five warps share each SM sub-partition's register file); more warps to keep the FP64 pipe fed
-constexpr int kWPCWide = 20;
 constexpr int kWPC32 = 24;    // f32: 24 warps x 2 stages x 4.2 KB per SM
 constexpr int kWPC32L1 = 20;  // f32, L1-leaning: 20 warps, 168 KB of stages
 constexpr int kStages = 2;
@@ -420,19 +417,6 @@ cudaError_t set_smem_attr() {
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes16);
 }
 
-// The same for a launch that exists only with 16-bit column offsets.
-template <typename VT, int SIGMA, int WPC, int STAGES, bool DOT>
-cudaError_t set_smem_attr16() {
-    static_assert(smem_bytes<VT, SIGMA, WPC, STAGES, true>() <= kMaxDynSmem, "stages exceed shared memory");
-    const int bytes16 = (int)smem_bytes<VT, SIGMA, WPC, STAGES, true>();
-    cudaError_t e;
-    if ((e = cudaFuncSetAttribute(k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXReadOnly, true>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes16)) != cudaSuccess)
-        return e;
-    return cudaFuncSetAttribute(k_spmv<VT, SIGMA, WPC, STAGES, DOT, kXStream, true>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, bytes16);
-}
-
 }  // namespace
 
 // Sets the dynamic shared-memory limit of every SpMV kernel once per process (before any graph
@@ -445,8 +429,6 @@ int prepare_spmv_kernels() {
     DG_CUDA((set_smem_attr<double, 16, kWPC, kStages, true>()));
     DG_CUDA((set_smem_attr<double, 16, kWPCL1, kStages, false>()));
     DG_CUDA((set_smem_attr<double, 16, kWPCL1, kStages, true>()));
-    DG_CUDA((set_smem_attr16<double, 16, kWPCWide, kStages, false>()));
-    DG_CUDA((set_smem_attr16<double, 16, kWPCWide, kStages, true>()));
     DG_CUDA((set_smem_attr<float, 16, kWPC32, kStages, false>()));
     DG_CUDA((set_smem_attr<float, 16, kWPC32, kStages, true>()));
     DG_CUDA((set_smem_attr<float, 16, kWPC32L1, kStages, false>()));
@@ -486,7 +468,7 @@ int calibrator_init(dimgpu_calibrator* c, const dimgpu_csr5* m) {
     // slots for every launch configuration the matrix may use, so that pinning another keeps it valid
     const int sms = device_sm_count(m->device);
     uint32_t most = std::max(m->plan.nwarps, m->plan32.nwarps);
-    for (int w : {kWPC, kWPCL1, kWPCWide, kWPC32, kWPC32L1})
+    for (int w : {kWPC, kWPCL1, kWPC32, kWPC32L1})
         most = std::max(most, make_spmv_plan(m->tile_count, sms, w).nwarps);
     c->nslots = std::max<uint32_t>(most, 1);
     DG_CHECK(dev_alloc_n(&c->cal_val, c->nslots));
@@ -530,12 +512,6 @@ int launch_spmv_f64(const dimgpu_csr5* m, const double* x, double* y, dimgpu_cal
         if (m->plan.warps_per_cta == kWPCL1)
             return dot ? launch_idx<double, 16, kWPCL1, kStages, true>(m, m->vals, x, y, cal, ep, stream)
                        : launch_idx<double, 16, kWPCL1, kStages, false>(m, m->vals, x, y, cal, ep, stream);
-        if (m->plan.warps_per_cta == kWPCWide) {
-            if (!m->col16)
-                return fail(DIMGPU_ERR_UNSUPPORTED, "the %d-warp launch needs 16-bit column offsets", kWPCWide);
-            return dot ? launch_cfg<double, 16, kWPCWide, kStages, true, true>(m, m->vals, x, y, cal, ep, stream)
-                       : launch_cfg<double, 16, kWPCWide, kStages, false, true>(m, m->vals, x, y, cal, ep, stream);
-        }
         return dot ? launch_idx<double, 16, kWPC, kStages, true>(m, m->vals, x, y, cal, ep, stream)
                    : launch_idx<double, 16, kWPC, kStages, false>(m, m->vals, x, y, cal, ep, stream);
     default:
@@ -571,7 +547,7 @@ int time_configs(dimgpu_csr5* m, int nconf, Set set, cudaStream_t stream, int* c
     DG_CHECK(dev_alloc_n(&x, m->cols));
     int rc = dev_alloc_n(&y, m->rows);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    float best[6] = {1e30f, 1e30f, 1e30f, 1e30f, 1e30f, 1e30f};
+    float best[4] = {1e30f, 1e30f, 1e30f, 1e30f};
     if (rc == DIMGPU_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
         rc = cuda_fail(cudaGetLastError(), "cudaEventCreate");
     if (rc == DIMGPU_OK) {
@@ -585,7 +561,7 @@ int time_configs(dimgpu_csr5* m, int nconf, Set set, cudaStream_t stream, int* c
                 rc = cuda_fail(cudaGetLastError(), "x = 1");
         }
     }
-    for (int i = 0; i < nconf && i < 6 && rc == DIMGPU_OK; ++i) {
+    for (int i = 0; i < nconf && i < 4 && rc == DIMGPU_OK; ++i) {
         set(i);
         for (int rep = 0; rep < 3 && rc == DIMGPU_OK; ++rep) {
             cudaEventRecord(e0, stream);
@@ -604,7 +580,7 @@ int time_configs(dimgpu_csr5* m, int nconf, Set set, cudaStream_t stream, int* c
     if (rc == DIMGPU_OK)
         rc = check_status(m->own_cal, stream);
     int b = 0;
-    for (int i = 1; i < nconf && i < 6; ++i)
+    for (int i = 1; i < nconf && i < 4; ++i)
         if (best[i] < best[b])
             b = i;
     *chosen = (b != 0 && best[b] < 0.97f * best[0]) ? b : 0;
@@ -624,14 +600,14 @@ int autotune_gathers(dimgpu_csr5* m, cudaStream_t stream) {
     if (m->tile_count < 4096 || m->rows == 0 || m->cols == 0)
         return DIMGPU_OK;
     const int sms = device_sm_count(m->device);
-    const int wpc[3] = {kWPC, kWPCL1, kWPCWide};
+    const int wpc[2] = {kWPC, kWPCL1};
     const int mode[2] = {kXReadOnly, kXStream};
     auto set = [&](int i) {
         m->plan = make_spmv_plan(m->tile_count, sms, wpc[i / 2]);
         m->x_mode = mode[i % 2];
     };
     int c = 0;
-    const int rc = time_configs<double>(m, m->col16 ? 6 : 4, set, stream, &c);
+    const int rc = time_configs<double>(m, 4, set, stream, &c);
     set(rc == DIMGPU_OK ? c : 0);
     return rc;
 }
@@ -825,11 +801,9 @@ extern "C" int dimgpu_csr5_set_spmv_launch(dimgpu_csr5* m, int f32, uint32_t war
         return fail(DIMGPU_ERR_INVALID_ARGUMENT, "gather mode %d", gather);
     const int wa = f32 ? kWPC32 : kWPC;
     const int wb = f32 ? kWPC32L1 : kWPCL1;
-    const bool wide = !f32 && warps_per_cta == (uint32_t)kWPCWide && m->col16;
-    if (warps_per_cta != (uint32_t)wa && warps_per_cta != (uint32_t)wb && !wide)
-        return fail(DIMGPU_ERR_INVALID_ARGUMENT,
-                    "%u warps per CTA is not an %s SpMV launch of this matrix (%d or %d%s)", warps_per_cta,
-                    f32 ? "f32" : "f64", wa, wb, (!f32 && m->col16) ? ", or 20" : "");
+    if (warps_per_cta != (uint32_t)wa && warps_per_cta != (uint32_t)wb)
+        return fail(DIMGPU_ERR_INVALID_ARGUMENT, "%u warps per CTA is not an %s SpMV launch (%d or %d)",
+                    warps_per_cta, f32 ? "f32" : "f64", wa, wb);
     const spmv_plan pl = make_spmv_plan(m->tile_count, device_sm_count(m->device), (int)warps_per_cta);
     const int mode = gather == DIMGPU_GATHER_STREAM ? kXStream : kXReadOnly;
     if (f32) {

@@ -39,52 +39,33 @@ struct tile_geom {
     static constexpr uint64_t FMASK = (SIGMA == 64) ? ~0ull : ((1ull << SIGMA) - 1);
 };
 
-// Column indices of lane `lane`'s column, read from a shared stage.  16-bit offsets stay packed two per
-// word (rows 2w and 2w + 1 of word w, quad order of layout.cuh) and are added to the tile's base column
-// when a gather needs them, so a column holds 8 registers of indices instead of 16.
-template <int SIGMA, bool IDX16>
-struct column_index {
-    static constexpr int N = IDX16 ? SIGMA / 2 : SIGMA;
-    uint32_t w[N];
-    uint32_t base;
-
-    __device__ __forceinline__ void load(const unsigned char* cols, unsigned lane, uint32_t col_base) {
-        base = col_base;
-        if constexpr (IDX16) {
-            const uint2* sc = reinterpret_cast<const uint2*>(cols);
-#pragma unroll
-            for (int j = 0; j < SIGMA / 4; ++j) {
-                const uint2 q = sc[j * 32 + lane];  // four u16 in quad order
-                w[2 * j + 0] = q.x;
-                w[2 * j + 1] = q.y;
-            }
-        } else {
-            const uint4* sc = reinterpret_cast<const uint4*>(cols);
-#pragma unroll
-            for (int j = 0; j < SIGMA / 4; ++j) {
-                const uint4 q = sc[j * 32 + lane];
-                w[4 * j + 0] = q.x;
-                w[4 * j + 1] = q.y;
-                w[4 * j + 2] = q.z;
-                w[4 * j + 3] = q.w;
-            }
-        }
-    }
-    __device__ __forceinline__ uint32_t operator[](int r) const {
-        if constexpr (IDX16)
-            return base + ((r & 1) ? (w[r >> 1] >> 16) : (w[r >> 1] & 0xFFFFu));
-        else
-            return w[r];
-    }
-};
-
 // Loads lane `lane`'s column (SIGMA values and column indices) from a shared stage; 16-bit indices are
 // offsets from `col_base`.
 template <typename VT, int SIGMA, bool IDX16 = false>
 __device__ __forceinline__ void load_column(const unsigned char* stage, unsigned lane, uint32_t col_base,
-                                            VT (&v)[SIGMA], column_index<SIGMA, IDX16>& ci) {
+                                            VT (&v)[SIGMA], uint32_t (&ci)[SIGMA]) {
     using G = tile_geom<VT, SIGMA, IDX16>;
-    ci.load(stage + G::VBYTES, lane, col_base);
+    if constexpr (IDX16) {
+        const uint2* sc = reinterpret_cast<const uint2*>(stage + G::VBYTES);
+#pragma unroll
+        for (int j = 0; j < SIGMA / 4; ++j) {
+            const uint2 q = sc[j * 32 + lane];  // four u16 in quad order
+            ci[4 * j + 0] = col_base + (q.x & 0xFFFFu);
+            ci[4 * j + 1] = col_base + (q.x >> 16);
+            ci[4 * j + 2] = col_base + (q.y & 0xFFFFu);
+            ci[4 * j + 3] = col_base + (q.y >> 16);
+        }
+    } else {
+        const uint4* sc = reinterpret_cast<const uint4*>(stage + G::VBYTES);
+#pragma unroll
+        for (int j = 0; j < SIGMA / 4; ++j) {
+            const uint4 q = sc[j * 32 + lane];
+            ci[4 * j + 0] = q.x;
+            ci[4 * j + 1] = q.y;
+            ci[4 * j + 2] = q.z;
+            ci[4 * j + 3] = q.w;
+        }
+    }
     if constexpr (sizeof(VT) == 8) {
         const double2* sv = reinterpret_cast<const double2*>(stage);
 #pragma unroll
@@ -105,10 +86,6 @@ __device__ __forceinline__ void load_column(const unsigned char* stage, unsigned
         }
     }
 }
-
-// x gathers in flight ahead of their products per lane (see process_tile).
-template <typename VT, int SIGMA>
-constexpr int kGatherAhead = sizeof(VT) == 8 ? (SIGMA < 8 ? SIGMA : 8) : SIGMA;
 
 // The carry chain of one warp over its run of tiles (values uniform across the lanes).
 template <typename VT>
@@ -173,21 +150,13 @@ __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned cha
     const Word* sd = reinterpret_cast<const Word*>(st + G::VBYTES + G::CBYTES);
 
     VT v[SIGMA];
-    column_index<SIGMA, IDX16> ci;
+    uint32_t ci[SIGMA];
     load_column<VT, SIGMA, IDX16>(st, lane, col_base, v, ci);
     const Word w = sd[lane];
-    // x gathers run AHEAD rows ahead of the products that use them: the f32 product (latency-bound) issues
-    // all of them at once; the FP64 product, whose warps wait on the FP64 pipe between products, keeps
-    // fewer in flight and so fewer registers, which lets more warps share an SM.
-    constexpr int AHEAD = kGatherAhead<VT, SIGMA>;
     VT xv[SIGMA];
 #pragma unroll
-    for (int r = 0; r < AHEAD; ++r)
+    for (int r = 0; r < SIGMA; ++r)
         xv[r] = load_x<XM>(io.x + ci[r], pol_keep);
-    auto gather_ahead = [&](int r) {
-        if (r + AHEAD < SIGMA)
-            xv[r + AHEAD] = load_x<XM>(io.x + ci[r + AHEAD], pol_keep);
-    };
     // the fused dot needs x at this tile's rows: fetch them now, off the write-out's path
     VT xrow = VT(0);
     if constexpr (DOT) {
@@ -210,10 +179,8 @@ __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned cha
         // partition_fast_track (csr5.h:562-574): the whole tile is one row
         VT acc = VT(0);
 #pragma unroll
-        for (int r = 0; r < SIGMA; ++r) {
-            gather_ahead(r);
+        for (int r = 0; r < SIGMA; ++r)
             acc = fma(v[r], xv[r], acc);
-        }
         H = warp_sum(acc);
         Lt = H;
         K = 1;
@@ -235,7 +202,6 @@ __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned cha
             // is applied afterwards; every sum is the same chain of fma as in the general loop.
 #pragma unroll
             for (int r = 0; r < SIGMA; ++r) {
-                gather_ahead(r);
                 const bool bit = ((flag >> r) & 1u) != 0;
                 red = bit ? sum : red;
                 sum = bit ? VT(0) : sum;
@@ -253,7 +219,6 @@ __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned cha
         } else {
 #pragma unroll
             for (int r = 0; r < SIGMA; ++r) {
-                gather_ahead(r);
                 const bool bit = ((fl >> r) & 1u) != 0;
                 const bool close = bit && seen;
                 if (close)

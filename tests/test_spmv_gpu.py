@@ -229,8 +229,7 @@ def _launch_matrices(rng):
     yield random_csr(rng, 3000, 3000, 2.0)
 
 
-@pytest.mark.parametrize("warps,gather", [(16, "l1"), (16, "stream"), (12, "l1"), (12, "stream"), (20, "l1"),
-                                          (20, "stream")])
+@pytest.mark.parametrize("warps,gather", [(16, "l1"), (16, "stream"), (12, "l1"), (12, "stream")])
 def test_every_f64_launch_configuration(native, torch_cuda, warps, gather):
     """Each f64 launch the per-matrix timing may choose, pinned: the product, the product with the fused
     dot, and a CG solve."""
@@ -244,10 +243,6 @@ def test_every_f64_launch_configuration(native, torch_cuda, warps, gather):
     for m in _launch_matrices(rng):
         n = m.dimensions.rows
         A = csr5.from_csr(m)
-        if warps == 20 and A.device_bytes < 12 * m.nnz + 2 * A.tile_count * 512:
-            with pytest.raises(ValueError):  # no 16-bit column offsets: the 20-warp launch does not exist
-                A.set_spmv_launch(warps, gather)
-            continue
         A.set_spmv_launch(warps, gather)
         assert A.spmv_launch() == (warps, gather)
         x = rng.uniform(-1, 1, n)
@@ -307,7 +302,7 @@ def test_every_f32_launch_configuration(native, torch_cuda, warps, gather):
 def test_launch_configuration_errors(native, torch_cuda):
     A = csr5.from_csr(random_csr(np.random.default_rng(1), 500, 500, 5.0))
     with pytest.raises(ValueError):
-        A.set_spmv_launch(24)  # an f32 launch, not an f64 one
+        A.set_spmv_launch(20)  # an f32 launch, not an f64 one
     with pytest.raises(ValueError):
         A.set_spmv_launch(16, f32=True)
     with pytest.raises(ValueError):
