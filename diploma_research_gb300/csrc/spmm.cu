@@ -19,8 +19,9 @@
 // for the in-order carry chain -- the same left-to-right sums as the SpMV.
 //
 // The optional epilogue of the block CG computes, per right-hand side, dot_j = sum_i X[i,j] Y[i,j]
-// (products and per-tile partial sums in the value type, accumulated in f64 across tiles and CTAs in
-// a fixed order) and alpha_j = rr_j / dot_j (columns whose mask is clear are skipped).
+// (products in the value type, sums in f64, in a fixed order: each warp reads back the rows it finished
+// in a chunk once the chunk is done, the lane groups taking rows in turn) and alpha_j = rr_j / dot_j
+// (columns whose mask is clear are skipped).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -195,6 +196,30 @@ __device__ __forceinline__ void st_vec(VT* p, const vv<VT, V>& v) {
     }
 }
 
+// Coherent load of V consecutive values this kernel wrote (read back past L1).
+template <typename VT, int V>
+__device__ __forceinline__ vv<VT, V> ldcg_vec(const VT* p) {
+    vv<VT, V> r;
+    if constexpr (V == 1) {
+        r.a[0] = __ldcg(p);
+    } else if constexpr (sizeof(VT) == 4 && V == 2) {
+        const float2 f = __ldcg(reinterpret_cast<const float2*>(p));
+        r.a[0] = f.x;
+        r.a[1] = f.y;
+    } else if constexpr (sizeof(VT) == 4 && V == 4) {
+        const float4 f = __ldcg(reinterpret_cast<const float4*>(p));
+        r.a[0] = f.x;
+        r.a[1] = f.y;
+        r.a[2] = f.z;
+        r.a[3] = f.w;
+    } else {
+#pragma unroll
+        for (int h = 0; h < V; ++h)
+            r.a[h] = __ldcg(p + h);
+    }
+    return r;
+}
+
 // Y = A X.  KP = k rounded up to 8, 16 or 32; each lane holds V consecutive right-hand sides, so a lane
 // group has LG = KP / V lanes and a warp NG = 32 / LG groups; group g walks tile columns [g LG, (g+1) LG).
 template <typename VT, int KP, int V, int WPC, int STAGES, bool DOT>
@@ -243,20 +268,20 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
 #pragma unroll
     for (int i = 0; i < V; ++i)
         dot_acc[i] = 0.0;
-    W tdot = vv_zero<VT, V>();  // this tile's share of the dot, folded into dot_acc once per tile
+    // rows this warp wrote in the current chunk (the dot epilogue reads them back once the chunk is done)
+    uint32_t wr_lo = 0xFFFFFFFFu, wr_hi = 0u;
     bool open = false, cal_valid = false;
     W carry = vv_zero<VT, V>(), cal = vv_zero<VT, V>();
     uint32_t carry_row = 0, cal_row = 0;
 
-    // k-wide row write by the lanes of one group (`mine`), with its share of the dot
+    // k-wide row write by the lanes of one group (`mine`); with the dot epilogue, the row is remembered
     auto put_row = [&](bool mine, uint32_t row, const W& val) {
-        if (mine && active) {
-            st_vec<VT, V>(Yl + (uint64_t)row * ldy, val);
+        if (mine) {
+            if (active)
+                st_vec<VT, V>(Yl + (uint64_t)row * ldy, val);
             if constexpr (DOT) {
-                const W xr = ldg_vec<VT, V>(Xl + (uint64_t)row * ldx, pol_keep);
-#pragma unroll
-                for (int i = 0; i < V; ++i)
-                    tdot.a[i] = fma(val.a[i], xr.a[i], tdot.a[i]);
+                wr_lo = min(wr_lo, row);
+                wr_hi = max(wr_hi, row);
             }
         }
     };
@@ -447,13 +472,6 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
                     carry = Lt;
                     carry_row = row_last;
                 }
-                if constexpr (DOT) {
-    #pragma unroll
-                    for (int q = 0; q < V; ++q) {
-                        dot_acc[q] += (double)tdot.a[q];
-                        tdot.a[q] = VT(0);
-                    }
-                }
                 __syncwarp();
                 // refill this slot with the warp's tile STAGES positions ahead (this chunk or its next one)
                 const uint64_t tn = seq_tile(q + STAGES);
@@ -526,12 +544,35 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
                 }
                 put_row(g == 0, cal_row, vv_sum<VT, V>(v, cal));
             }
+            if constexpr (DOT) {
+                // x.y over the rows this chunk finished -- a contiguous range, read back once the chunk is
+                // done, the lane groups taking rows in turn so that every warp instruction serves NG rows
+                // (accumulating at each row write would issue one FP64 instruction per row for one group)
+                uint32_t lo = wr_lo, hi = wr_hi;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    lo = min(lo, __shfl_xor_sync(kFull, lo, o));
+                    hi = max(hi, __shfl_xor_sync(kFull, hi, o));
+                }
+                __syncwarp();  // the rows' stores by the other lanes are visible to the loads below
+                for (uint32_t r = lo + g; lo <= hi && r <= hi; r += NG) {
+                    // empty rows were zeroed by whichever CTA reached them; they add nothing
+                    if (active && __ldg(&p.row_ptr[r]) != __ldg(&p.row_ptr[r + 1])) {
+                        const W yv = ldcg_vec<VT, V>(Yl + (uint64_t)r * ldy);
+                        const W xr = ldg_vec<VT, V>(Xl + (uint64_t)r * ldx, pol_keep);
+#pragma unroll
+                        for (int q = 0; q < V; ++q)
+                            dot_acc[q] += (double)(yv.a[q] * xr.a[q]);
+                    }
+                }
+                wr_lo = 0xFFFFFFFFu;
+                wr_hi = 0u;
+            }
         }
     }
     if constexpr (DOT) {
 #pragma unroll
         for (int q = 0; q < V; ++q) {
-            dot_acc[q] += (double)tdot.a[q];
             // sum over the groups (same right-hand sides), then per CTA in warp order
 #pragma unroll
             for (int o = LG; o < 32; o <<= 1)
