@@ -19,9 +19,12 @@
 // for the in-order carry chain -- the same left-to-right sums as the SpMV.
 //
 // The optional epilogue of the block CG computes, per right-hand side, dot_j = sum_i X[i,j] Y[i,j]
-// (products in the value type, sums in f64, in a fixed order: each warp reads back the rows it finished
-// in a chunk once the chunk is done, the lane groups taking rows in turn) and alpha_j = rr_j / dot_j
-// (columns whose mask is clear are skipped).
+// (products and per-tile partial sums in the value type, accumulated in f64 across tiles and CTAs in a
+// fixed order) and alpha_j = rr_j / dot_j (columns whose mask is clear are skipped).  With several lane
+// groups per warp the rows a tile finishes are read back right after it, while they are still cached,
+// the groups taking them in turn: every FP64 instruction then serves NG rows, where a product at each row
+// write would issue one for the single group that writes it.  With one group (the whole warp) the product
+// is taken at the row write.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -268,22 +271,73 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
 #pragma unroll
     for (int i = 0; i < V; ++i)
         dot_acc[i] = 0.0;
-    // rows this warp wrote in the current chunk (the dot epilogue reads them back once the chunk is done)
+    // dot epilogue: READBACK -- the rows this warp wrote in the current tile, read back after it; else the
+    // tile's products, taken at each row write
+    constexpr bool READBACK = NG > 1;
     uint32_t wr_lo = 0xFFFFFFFFu, wr_hi = 0u;
+    W tdot = vv_zero<VT, V>();
+    const bool no_empty = p.n_empty == 0;
     bool open = false, cal_valid = false;
     W carry = vv_zero<VT, V>(), cal = vv_zero<VT, V>();
     uint32_t carry_row = 0, cal_row = 0;
 
-    // k-wide row write by the lanes of one group (`mine`); with the dot epilogue, the row is remembered
+    // k-wide row write by the lanes of one group (`mine`), remembered or with its share of the dot
     auto put_row = [&](bool mine, uint32_t row, const W& val) {
         if (mine) {
-            if (active)
+            if (active) {
                 st_vec<VT, V>(Yl + (uint64_t)row * ldy, val);
-            if constexpr (DOT) {
+                if constexpr (DOT && !READBACK) {
+                    const W xr = ldg_vec<VT, V>(Xl + (uint64_t)row * ldx, pol_keep);
+#pragma unroll
+                    for (int q = 0; q < V; ++q)
+                        tdot.a[q] = fma(val.a[q], xr.a[q], tdot.a[q]);
+                }
+            }
+            if constexpr (DOT && READBACK) {
                 wr_lo = min(wr_lo, row);
                 wr_hi = max(wr_hi, row);
             }
         }
+    };
+    // the same for the (at most two) rows a chunk finishes after its last tile, with their share of the dot
+    auto put_row_dot = [&](bool mine, uint32_t row, const W& val) {
+        if (mine && active) {
+            st_vec<VT, V>(Yl + (uint64_t)row * ldy, val);
+            if constexpr (DOT) {
+                const W xr = ldg_vec<VT, V>(Xl + (uint64_t)row * ldx, pol_keep);
+#pragma unroll
+                for (int q = 0; q < V; ++q)
+                    dot_acc[q] += (double)(val.a[q] * xr.a[q]);
+            }
+        }
+    };
+    // x.y over the rows [lo, hi] one tile finished, four rows per group in flight, summed in the value type
+    // and folded into dot_acc.  Every non-empty row of the range was written by this warp in this tile:
+    // the rows between two rows the tile wrote have all their elements in it.
+    auto dot_rows = [&](uint32_t lo, uint32_t hi) {
+        W ts = vv_zero<VT, V>();
+#pragma unroll 1
+        for (uint32_t r0 = lo; r0 <= hi; r0 += 4 * NG) {
+            W yv[4], xr[4];
+            bool on[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t r = r0 + (uint32_t)u * NG + g;
+                // empty rows were zeroed by whichever CTA reached them; they add nothing
+                on[u] = active && r <= hi && (no_empty || __ldg(&p.row_ptr[r]) != __ldg(&p.row_ptr[r + 1]));
+                const uint32_t rr = r <= hi ? r : hi;
+                yv[u] = ldcg_vec<VT, V>(Yl + (uint64_t)rr * ldy);
+                xr[u] = ldg_vec<VT, V>(Xl + (uint64_t)rr * ldx, pol_keep);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int q = 0; q < V; ++q)
+                    ts.a[q] = fma(on[u] ? yv[u].a[q] : VT(0), xr[u].a[q], ts.a[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < V; ++q)
+            dot_acc[q] += (double)ts.a[q];
     };
 
     {
@@ -472,6 +526,20 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
                     carry = Lt;
                     carry_row = row_last;
                 }
+                if constexpr (DOT && READBACK) {
+                    const uint32_t lo = __reduce_min_sync(kFull, wr_lo), hi = __reduce_max_sync(kFull, wr_hi);
+                    wr_lo = 0xFFFFFFFFu;
+                    wr_hi = 0u;
+                    __syncwarp();  // the rows' stores by the other lanes are visible to the loads below
+                    if (lo <= hi)
+                        dot_rows(lo, hi);
+                } else if constexpr (DOT) {
+#pragma unroll
+                    for (int q = 0; q < V; ++q) {
+                        dot_acc[q] += (double)tdot.a[q];
+                        tdot.a[q] = VT(0);
+                    }
+                }
                 __syncwarp();
                 // refill this slot with the warp's tile STAGES positions ahead (this chunk or its next one)
                 const uint64_t tn = seq_tile(q + STAGES);
@@ -514,7 +582,7 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
             if (lane == 0)
                 st_release_u32(&p.flag[c], (epoch << 2) | kind);
             if (open && !cont_after)
-                put_row(g == 0, carry_row, carry);
+                put_row_dot(g == 0, carry_row, carry);
             if (cal_valid && (!through || !cont_after)) {
                 // look back for the chunk where cal_row began, then add the fragments in chunk order
                 uint32_t first = (uint32_t)c;
@@ -542,31 +610,7 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
                         v.a[q] = a;
                     }
                 }
-                put_row(g == 0, cal_row, vv_sum<VT, V>(v, cal));
-            }
-            if constexpr (DOT) {
-                // x.y over the rows this chunk finished -- a contiguous range, read back once the chunk is
-                // done, the lane groups taking rows in turn so that every warp instruction serves NG rows
-                // (accumulating at each row write would issue one FP64 instruction per row for one group)
-                uint32_t lo = wr_lo, hi = wr_hi;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    lo = min(lo, __shfl_xor_sync(kFull, lo, o));
-                    hi = max(hi, __shfl_xor_sync(kFull, hi, o));
-                }
-                __syncwarp();  // the rows' stores by the other lanes are visible to the loads below
-                for (uint32_t r = lo + g; lo <= hi && r <= hi; r += NG) {
-                    // empty rows were zeroed by whichever CTA reached them; they add nothing
-                    if (active && __ldg(&p.row_ptr[r]) != __ldg(&p.row_ptr[r + 1])) {
-                        const W yv = ldcg_vec<VT, V>(Yl + (uint64_t)r * ldy);
-                        const W xr = ldg_vec<VT, V>(Xl + (uint64_t)r * ldx, pol_keep);
-#pragma unroll
-                        for (int q = 0; q < V; ++q)
-                            dot_acc[q] += (double)(yv.a[q] * xr.a[q]);
-                    }
-                }
-                wr_lo = 0xFFFFFFFFu;
-                wr_hi = 0u;
+                put_row_dot(g == 0, cal_row, vv_sum<VT, V>(v, cal));
             }
         }
     }
