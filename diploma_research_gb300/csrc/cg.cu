@@ -134,6 +134,42 @@ __device__ __forceinline__ void vloop(uint64_t nv, Ld load, Op op) {
     }
 }
 
+// Visits every vector index i in [0, nv) in the same per-thread order as vloop, software-pipelined:
+// rounds of U indices one grid stride apart, with round k+1's loads issued before round k's ops, so that
+// the next round's loads are in flight while the FP64 pipe works through the current one (with a
+// vector kernel's 2 DFMA per element the pipe is busy for about as long as the loads take).  load(i, slot)
+// and op(i, slot) use slots [0, U) and [U, 2U) in turn; indices at or past nv are skipped, so a last
+// partial round costs one memory round trip, not one per index.
+template <int U, typename Ld, typename Op>
+__device__ __forceinline__ void vloop_pipe(uint64_t nv, Ld load, Op op) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t span = U * stride;
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    auto ld_round = [&](uint64_t i0, int base) {
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (i0 + u * stride < nv)
+                load(i0 + u * stride, base + u);
+    };
+    auto op_round = [&](uint64_t i0, int base) {
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (i0 + u * stride < nv)
+                op(i0 + u * stride, base + u);
+    };
+    ld_round(i, 0);
+    while (i < nv) {
+        ld_round(i + span, U);
+        op_round(i, 0);
+        i += span;
+        if (i >= nv)
+            break;
+        ld_round(i + span, 0);
+        op_round(i, U);
+        i += span;
+    }
+}
+
 // The scalar elements past the last full vector, visited by the first threads of block 0.
 template <typename F>
 __device__ __forceinline__ void vtail(uint64_t n, uint64_t width, F f) {
@@ -203,8 +239,9 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_update_r64(const double* As,
     }
     const uint64_t pol = policy_evict_last();
     double rr = 0;
-    double2 av[kUnroll], qv[kUnroll];
-    vloop(
+    constexpr int U = 2;
+    double2 av[2 * U], qv[2 * U];
+    vloop_pipe<U>(
         n / 2,
         [&](uint64_t i, int u) {
             av[u] = ld2_keep(As + 2 * i, pol);
@@ -250,10 +287,10 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_update_xs64(double* x, doubl
         return;
     const uint64_t pol = policy_evict_last();
     const bool more = !stop;
-    constexpr int U = 3;  // three 16-byte loads per element: 36 registers of loaded data per round
-    double2 sv[U], xv[U], rv[U];
+    constexpr int U = 1;  // three 16-byte loads per element, two rounds in flight: 24 registers of data
+    double2 sv[2 * U], xv[2 * U], rv[2 * U];
     if (more) {
-        vloop<U>(
+        vloop_pipe<U>(
             n / 2,
             [&](uint64_t i, int u) {
                 sv[u] = ld2_keep(s + 2 * i, pol);
@@ -271,7 +308,7 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_update_xs64(double* x, doubl
             s[i] = fma(beta, si, r[i]);
         });
     } else {
-        vloop<U>(
+        vloop_pipe<U>(
             n / 2,
             [&](uint64_t i, int u) {
                 sv[u] = ld2_keep(s + 2 * i, pol);
@@ -359,9 +396,9 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_update_r_mixed(const float* 
     }
     const uint64_t pol = policy_evict_last();
     double rr = 0;
-    constexpr int U = 2;  // four 16-byte loads per element
-    float4 av[U], sv[U], qv[U], yv[U];
-    vloop<U>(
+    constexpr int U = 1;  // four 16-byte loads per element, two rounds in flight
+    float4 av[2 * U], sv[2 * U], qv[2 * U], yv[2 * U];
+    vloop_pipe<U>(
         n / 4,
         [&](uint64_t i, int u) {
             av[u] = ld4_keep(As + 4 * i, pol);
@@ -487,8 +524,9 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_update_s_mixed(float* s, con
     if (stop || (after_ru ? no_ru != 0u : no_ru == 0u))
         return;
     const uint64_t pol = policy_evict_last();
-    float4 sv[kUnroll], rv[kUnroll];
-    vloop(
+    constexpr int U = 1;
+    float4 sv[2 * U], rv[2 * U];
+    vloop_pipe<U>(
         n / 4,
         [&](uint64_t i, int u) {
             sv[u] = ld4_keep(s + 4 * i, pol);
