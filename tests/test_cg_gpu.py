@@ -52,13 +52,16 @@ def test_fp64_cg_vs_oracle(native, engine, use_graph):
     np.testing.assert_allclose(x, xs, rtol=0, atol=1e-6)
 
 
-def test_graph_and_host_loop_agree_bitwise(native):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_graph_and_host_loop_agree_bitwise(native, precision):
+    """The graph (device-side WHILE loop; for mixed, the reliable update as an IF node beside the s
+    update) and the host-driven loop launch the same kernels: same bits."""
     m = laplacian_2d_5pt(48)
     _, b = rhs(m, 1)
     A = csr5.from_csr(m)
-    x1, r1 = cg(A, b, tol=1e-9, use_graph=True, engine="graph")
-    x2, r2 = cg(A, b, tol=1e-9, use_graph=False)
-    assert r1.iterations == r2.iterations
+    x1, r1 = cg(A, b, tol=1e-9, use_graph=True, engine="graph", precision=precision)
+    x2, r2 = cg(A, b, tol=1e-9, use_graph=False, precision=precision)
+    assert r1.iterations == r2.iterations and r1.reliable_updates == r2.reliable_updates
     assert np.array_equal(x1, x2)
 
 

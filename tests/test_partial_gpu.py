@@ -118,7 +118,8 @@ def test_multi_rank_cg(native, torch_cuda, world):
     n = m.dimensions.rows
     xs = np.random.default_rng(3).uniform(-1, 1, n)
     port = _free_port()
-    with mp.Manager() as mgr:
+    # the manager process is started with spawn as well: this process has already initialised CUDA
+    with mp.get_context("spawn").Manager() as mgr:
         out = mgr.dict()
         mp.spawn(_cg_rank, args=(world, port, out), nprocs=world, join=True)
         res = [out[r] for r in range(world)]
