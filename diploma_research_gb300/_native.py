@@ -22,6 +22,7 @@ ERR_BREAKDOWN = -5
 ERR_NOT_CONVERGED = -6
 ERR_UNSUPPORTED = -7
 ERR_BAD_INDEX = -8
+ERR_IO = -9
 
 MEM_HOST = 0
 MEM_DEVICE = 1
@@ -132,6 +133,16 @@ _SIGNATURES = {
     "dimgpu_static_scratch_status": [_vp],
     "dimgpu_csr5_spmv_static_scratch": [_vp, _vp, _vp, _vp],
     "dimgpu_version": [],
+    "dimgpu_h5_csr_dimensions": [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_u32), ctypes.POINTER(_u32),
+                                 ctypes.POINTER(_u64)],
+    "dimgpu_h5_read_matlab_compatible": [ctypes.c_char_p, ctypes.c_char_p, _vp, _vp, _vp],
+    "dimgpu_h5_write_matlab_compatible": [ctypes.c_char_p, ctypes.c_char_p, _u32, _u32, _u64, _vp, _vp, _vp,
+                                          ctypes.c_int],
+    "dimgpu_h5_store_csr5": [ctypes.c_char_p, ctypes.c_char_p, _vp, ctypes.c_int],
+    "dimgpu_h5_load_csr5": [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(csr5_options), _vp, ctypes.POINTER(_vp)],
+    "dimgpu_h5_vector_length": [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_u64)],
+    "dimgpu_h5_read_vector": [ctypes.c_char_p, ctypes.c_char_p, _vp],
+    "dimgpu_h5_write_vector": [ctypes.c_char_p, ctypes.c_char_p, _u64, _vp, ctypes.c_int],
 }
 
 

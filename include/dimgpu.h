@@ -43,6 +43,7 @@ extern "C" {
 #define DIMGPU_ERR_NOT_CONVERGED (-6)    /* CG: max_it reached before the tolerance */
 #define DIMGPU_ERR_UNSUPPORTED (-7)
 #define DIMGPU_ERR_BAD_INDEX (-8)        /* a device-side bounds check failed */
+#define DIMGPU_ERR_IO (-9)               /* a file could not be read or written, or is outside the HDF5 subset */
 
 typedef struct dimgpu_csr5 dimgpu_csr5;             /* device CSR5 matrix */
 typedef struct dimgpu_calibrator dimgpu_calibrator; /* scratch of one SpMV at a time */
@@ -275,6 +276,43 @@ DIMGPU_API int dimgpu_cg_adjoint(const dimgpu_csr5* m, const double* g, const do
                                  void* stream);
 
 /* ---- diagnostics ------------------------------------------------------------------------------ */
+
+/* ---- HDF5 matrix files ------------------------------------------------------------------------
+ * The reference's dim::io::h5 (include/dim/io/h5.h:62-115, libs/dim/io/h5.cpp:45-74) on files it
+ * writes with libhdf5, without libhdf5: the library reads and writes the part of the HDF5 format those
+ * files use (superblock 0/1, version-1 object headers, symbol-table groups, contiguous, compact and
+ * chunked 1-D datasets, the deflate filter; files written with libver "latest" are refused) and writes
+ * the layout libhdf5's default settings produce.  Host memory only; DIMGPU_ERR_IO on a file that cannot
+ * be read or written or lies outside that subset.  A writer with append != 0 keeps the other members
+ * of an existing file (it is read, then rewritten through a temporary file). */
+
+/* read_matlab_compatible (h5.h:72-90), first call: the sizes of the MATLAB-compatible CSR group
+ * `group` (datasets data, ir, jc; attribute MATLAB_sparse = column count). */
+DIMGPU_API int dimgpu_h5_csr_dimensions(const char* path, const char* group, uint32_t* rows, uint32_t* cols,
+                                        uint64_t* nnz);
+/* read_matlab_compatible, second call: row_ptr (rows + 1), col_indices and values (nnz each) into
+ * caller buffers; indices stored in wider integer types are narrowed to u32 (an error if one does not fit). */
+DIMGPU_API int dimgpu_h5_read_matlab_compatible(const char* path, const char* group, uint32_t* row_ptr,
+                                                uint32_t* col_indices, double* values);
+/* write_matlab_compatible (h5.h:62-70): replaces `group` (the whole file unless append). */
+DIMGPU_API int dimgpu_h5_write_matlab_compatible(const char* path, const char* group, uint32_t rows, uint32_t cols,
+                                                 uint64_t nnz, const uint32_t* row_ptr, const uint32_t* col_indices,
+                                                 const double* values, int append);
+/* store (h5.cpp:45-55): the reference's CSR5 group of a matrix converted with the reference layout
+ * (dimgpu_csr5_options sigma 16, omega 4): attribute column_count; vals, col_idx, row_ptr, tile_ptr,
+ * tile_desc (an array type of 4 u32 per tile), tile_desc_offset_ptr, tile_desc_offset. */
+DIMGPU_API int dimgpu_h5_store_csr5(const char* path, const char* group, const dimgpu_csr5* m, int append);
+/* load_csr5 (h5.cpp:57-74): reads a stored CSR5 group (sigma 16, omega 4), puts its transposed tiles
+ * back into CSR order (the inverse of csr5::transpose, csr5.h:463-493) and converts it on the device
+ * like dimgpu_csr5_from_csr with `opt` (NULL: the device layout the products run on). */
+DIMGPU_API int dimgpu_h5_load_csr5(const char* path, const char* group, const dimgpu_csr5_options* opt, void* stream,
+                                   dimgpu_csr5** out);
+/* The result vectors of benchmarks/csr5/dim/main.cpp:35-43 (f64 datasets): length, read (converted to
+ * f64), write (refused, DIMGPU_ERR_INVALID_ARGUMENT, when the dataset exists unless overwrite). */
+DIMGPU_API int dimgpu_h5_vector_length(const char* path, const char* dataset, uint64_t* n);
+DIMGPU_API int dimgpu_h5_read_vector(const char* path, const char* dataset, double* y);
+DIMGPU_API int dimgpu_h5_write_vector(const char* path, const char* dataset, uint64_t n, const double* y,
+                                      int overwrite);
 
 DIMGPU_API const char* dimgpu_last_error_string(void);
 /* ABI version of this library (2: status queries, SpMM shapes with lane grouping, no persistent CG engine). */

@@ -12,6 +12,9 @@
 //   csr5::create_calibrator() (csr5.h:809)             csr5::create_calibrator()
 //   csr5::tail_partition_start(), non_zero_count()     the same names
 //   the dim_sp CG loop                                 dim::gpu::cg_solver
+//   dim::io::h5::read_matlab_compatible,               dim::gpu::io::read_matlab_compatible,
+//     write_matlab_compatible, load_csr5, store          write_matlab_compatible, load_csr5, store
+//     (include/dim/io/h5.h:62-115)                       (HDF5 files without libhdf5; see dimgpu.h)
 //
 // from_csr takes any matrix type with the members of dim::mat::csr<double> (csr.h:19-40):
 // `dimensions.rows`, `dimensions.cols`, and contiguous `values`, `row_start_offsets` (u32) and
@@ -28,6 +31,7 @@
 #include <stdexcept>
 #include <string>
 #include <utility>
+#include <vector>
 
 #include "dimgpu.h"
 
@@ -142,6 +146,15 @@ public:
         check(dimgpu_csr5_status(h_, cal ? cal->handle() : nullptr, stream));
     }
 
+    // Takes ownership of a handle made by the C ABI (dimgpu_csr5_from_csr, dimgpu_h5_load_csr5, ...).
+    static csr5 adopt(dimgpu_csr5* h) {
+        csr5 r;
+        r.h_ = h;
+        if (h)
+            check(dimgpu_csr5_get_info(h, &r.info_));
+        return r;
+    }
+
     calibrator create_calibrator() const {
         dimgpu_calibrator* c = nullptr;
         check(dimgpu_calibrator_create(h_, &c));
@@ -213,5 +226,70 @@ private:
     dimgpu_cg_solver* h_{};
     size_t rows_{};
 };
+
+// The reference's HDF5 matrix IO (dim::io::h5, include/dim/io/h5.h:62-115; libs/dim/io/h5.cpp:45-74).
+// File errors throw dim::gpu::error with DIMGPU_ERR_IO, a missing group std::invalid_argument.
+namespace io {
+
+// A CSR matrix with the members of dim::mat::csr<double> (csr.h:19-40).
+struct csr_matrix {
+    dimensions_t dimensions;
+    std::vector<double> values;
+    std::vector<uint32_t> row_start_offsets;
+    std::vector<uint32_t> col_indices;
+};
+
+// read_matlab_compatible (h5.h:72-90): datasets data, ir, jc and the attribute MATLAB_sparse.
+inline csr_matrix read_matlab_compatible(const std::string& path, const std::string& group = "A") {
+    uint32_t rows = 0, cols = 0;
+    uint64_t nnz = 0;
+    check(dimgpu_h5_csr_dimensions(path.c_str(), group.c_str(), &rows, &cols, &nnz));
+    csr_matrix m{{rows, cols}, std::vector<double>(nnz), std::vector<uint32_t>(size_t(rows) + 1),
+                 std::vector<uint32_t>(nnz)};
+    check(dimgpu_h5_read_matlab_compatible(path.c_str(), group.c_str(), m.row_start_offsets.data(),
+                                           m.col_indices.data(), m.values.data()));
+    return m;
+}
+
+// write_matlab_compatible (h5.h:62-70) of any matrix with the members of dim::mat::csr<double>.
+template <typename Csr>
+void write_matlab_compatible(const std::string& path, const std::string& group, const Csr& m, bool append = false) {
+    const auto nnz = static_cast<uint64_t>(std::size(m.values));
+    if (std::size(m.col_indices) != nnz || std::size(m.row_start_offsets) != size_t(m.dimensions.rows) + 1)
+        throw std::invalid_argument("csr arrays do not match the matrix dimensions");
+    check(dimgpu_h5_write_matlab_compatible(path.c_str(), group.c_str(), static_cast<uint32_t>(m.dimensions.rows),
+                                            static_cast<uint32_t>(m.dimensions.cols), nnz, std::data(m.row_start_offsets),
+                                            nnz ? std::data(m.col_indices) : nullptr, nnz ? std::data(m.values) : nullptr,
+                                            append ? 1 : 0));
+}
+
+// load_csr5 (h5.cpp:57-74): a stored CSR5 group, converted to the device layout (or `opt`'s).
+inline csr5 load_csr5(const std::string& path, const std::string& group = "A", const dimgpu_csr5_options* opt = nullptr,
+                      void* stream = nullptr) {
+    dimgpu_csr5* h = nullptr;
+    check(dimgpu_h5_load_csr5(path.c_str(), group.c_str(), opt, stream, &h));
+    return csr5::adopt(h);
+}
+
+// store (h5.cpp:45-55) of a matrix converted with the reference's layout (sigma 16, omega 4).
+inline void store(const std::string& path, const std::string& group, const csr5& m, bool append = false) {
+    check(dimgpu_h5_store_csr5(path.c_str(), group.c_str(), m.handle(), append ? 1 : 0));
+}
+
+// The result vectors of benchmarks/csr5/dim/main.cpp:35-43.
+inline std::vector<double> read_vector(const std::string& path, const std::string& dataset) {
+    uint64_t n = 0;
+    check(dimgpu_h5_vector_length(path.c_str(), dataset.c_str(), &n));
+    std::vector<double> y(n);
+    check(dimgpu_h5_read_vector(path.c_str(), dataset.c_str(), y.data()));
+    return y;
+}
+
+inline void write_vector(const std::string& path, const std::string& dataset, std::span<const double> y,
+                         bool overwrite = false) {
+    check(dimgpu_h5_write_vector(path.c_str(), dataset.c_str(), y.size(), y.data(), overwrite ? 1 : 0));
+}
+
+}  // namespace io
 
 }  // namespace dim::gpu

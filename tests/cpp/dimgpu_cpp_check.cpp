@@ -1,6 +1,7 @@
 // A C++ caller of dimgpu through include/dimgpu.hpp, as a dim user would write it: from_csr, spmv on
 // host spans and on device memory (CUDA runtime allocations, a stream, the status query), the CG
-// solver, and the reference's exceptions.
+// solver, the reference's exceptions, and the HDF5 matrix IO (write_matlab_compatible and
+// read_matlab_compatible, store and load_csr5, the result vector).
 //
 //   dimgpu_cpp_check <output file>
 //
@@ -118,6 +119,29 @@ int main(int argc, char** argv) {
     const dimgpu_cg_stats st = solver.solve(y, z);
     EXPECT(st.status == DIMGPU_OK && st.rel_residual <= 1.5e-10);
     A.status();
+
+    // HDF5 round trips next to the output file: the matrix through its MATLAB-compatible group and its
+    // CSR5 group (converted with the reference's layout), the solution as a result vector
+    const std::string h5path = std::string(argv[1]) + ".h5";
+    dim::gpu::io::write_matlab_compatible(h5path, "A", m);
+    const dim::gpu::io::csr_matrix back = dim::gpu::io::read_matlab_compatible(h5path, "A");
+    EXPECT(back.dimensions.rows == n && back.values == v && back.row_start_offsets == rp && back.col_indices == ci);
+    dimgpu_csr5_options ref_layout{16, 4, DIMGPU_LAYOUT_REFERENCE, 0};
+    const dim::gpu::csr5 R = dim::gpu::csr5::from_csr(back, &ref_layout);
+    dim::gpu::io::store(h5path, "A5", R, /*append=*/true);
+    const dim::gpu::csr5 L = dim::gpu::io::load_csr5(h5path, "A5");
+    std::vector<double> y5(n);
+    L.spmv(x, y5);
+    EXPECT(y5 == y);  // the same matrix, the same kernel: the same bits
+    dim::gpu::io::write_vector(h5path, "z", z);
+    EXPECT(dim::gpu::io::read_vector(h5path, "z") == z);
+    threw = false;
+    try {
+        (void)dim::gpu::io::read_matlab_compatible(h5path, "missing");
+    } catch (const std::invalid_argument&) {
+        threw = true;
+    }
+    EXPECT(threw);
 
     FILE* f = std::fopen(argv[1], "wb");
     EXPECT(f != nullptr);
