@@ -140,8 +140,7 @@ int vec_fill(uint64_t n, double v, double* y, cudaStream_t stream);
 
 // spmm.cu: CSR5 SpMM (lanes = right-hand sides, one pass takes k <= 32 columns)
 // SpMM shape codes the autotuner chooses from: bit 0 the launch shape (0: 8 warps x 3 stages, 1: 16 x 2),
-// bits 1-2 the lane grouping (0: the widest vector lanes the operands allow, 1: one right-hand side per
-// lane, 2: two per lane at k > 16)
+// bits 1-2 the lane grouping g (right-hand sides per lane: the widest the operands allow, >> g)
 constexpr int kSpmmShapes = 6;
 struct spmm_args {
     const void* X = nullptr;

@@ -4,16 +4,18 @@
 // by cp.async.bulk on an mbarrier ring, each warp owning a contiguous run of tiles, rows that cross runs
 // finished by a decoupled look-back, the CSR tail by the last CTA.
 //
-// Lanes.  KP = k rounded up to 8, 16 or 32.  Each lane holds V consecutive right-hand sides (f32: V = KP / 8
-// when k and the leading dimensions allow 8- or 16-byte vector accesses; else, and for FP64, V = 1), so a
-// lane group has LG = KP / V lanes and a warp G = 32 / LG groups; lane j of a group holds right-hand
+// Lanes.  KP = k rounded up to 8, 16 or 32.  Each lane holds V consecutive right-hand sides (f32: V = 4, 2
+// or 1, chosen by timing among those k and the leading dimensions allow with 16- or 8-byte vector
+// accesses; FP64: V = 1), so a lane group has LG = KP / V lanes and a warp G = 32 / LG groups; lane j of a
+// group holds right-hand
 // sides [j V, (j+1) V).  Group g walks the tile elements of tile columns [g LG, (g+1) LG) -- 16 LG consecutive
 // elements in CSR order -- one element per step: the element's value and column index come from shared
 // memory (16-byte loads of a whole tile column), every lane gathers X[col, jV .. jV+V) (one coalesced
 // k-wide row per group) and accumulates.  So one warp step does G elements x KP right-hand sides of
 // useful work: GB300's FP64 pipe (a warp-wide DFMA costs the same whatever the number of active lanes)
-// is kept full when k < 32, and with V > 1 the per-element overhead (flags, shared loads, shuffles) is
-// shared by four elements also at k = 16 and 32.  A set bit_flag bit closes the group's running row
+// is kept full when k < 32, and with V > 1 the per-element overhead (flags, shared loads, shuffles), which
+// bounds the f32 product (it is issue-bound), is paid once for V right-hand sides: a tile takes 16 LG
+// warp steps.  A set bit_flag bit closes the group's running row
 // (written as one k-wide Y row); after the tile the groups' head and tail sums are joined in group order
 // with shuffles, which finishes the rows that span groups and yields the tile's head and open segments
 // for the in-order carry chain -- the same left-to-right sums as the SpMV.
@@ -799,42 +801,35 @@ int mm_dispatch_kp(const dimgpu_csr5* m, const VT* vals, const spmm_args& a, con
     }
 }
 
-// Values per lane: KP / 8 (four lane groups of eight lanes) when k and the layout allow vector accesses
-// (k and both leading dimensions multiples of it, X and Y aligned to it); one value per lane otherwise.
+// The most values per lane the operands allow: 4 or 2 (16- or 8-byte vector accesses) when k and both
+// leading dimensions are multiples of it and X and Y are aligned to it, at most KP / 2 (a lane group keeps
+// two lanes); one value per lane otherwise.
 template <typename VT>
 int lanes_vec(const spmm_args& a, int kp) {
-    const int v = kp / 8;
-    if (v <= 1)
-        return 1;
-    const uintptr_t align = (uintptr_t)v * sizeof(VT);
-    const bool ok = a.k % v == 0 && a.ldx % v == 0 && a.ldy % v == 0 &&
-                    reinterpret_cast<uintptr_t>(a.X) % align == 0 && reinterpret_cast<uintptr_t>(a.Y) % align == 0;
-    return ok ? v : 1;
+    for (int v = std::min(4, kp / 2); v > 1; v /= 2) {
+        const uintptr_t align = (uintptr_t)v * sizeof(VT);
+        if (a.k % v == 0 && a.ldx % v == 0 && a.ldy % v == 0 && reinterpret_cast<uintptr_t>(a.X) % align == 0 &&
+            reinterpret_cast<uintptr_t>(a.Y) % align == 0)
+            return v;
+    }
+    return 1;
 }
 
 // Lane-group width for k right-hand sides.
 inline int kp_for(uint32_t k) { return k <= 8 ? 8 : (k <= 16 ? 16 : 32); }
 
-// Right-hand sides per lane that a shape code's lane grouping (bits 1-2) selects for these operands:
-// 0 the widest vector lanes the operands allow, 1 one per lane, 2 two per lane (k rounded to 32 with
-// at least two-wide vector access).  -1 when the grouping does not apply (it would repeat another).
+// Right-hand sides per lane that a shape code's lane grouping g (bits 1-2) selects for these operands: the
+// widest the operands allow (f32: 4, 2 or 1) shifted right by g -- g = 0 the widest, 1 half of it, 2 a
+// quarter.  -1 when that is below one (the grouping does not apply; it would repeat another).  FP64 keeps
+// one value per lane: it is bound by the FP64 pipe, which a warp DFMA occupies the same way whatever its
+// layout.
 template <typename VT>
 int lanes_for_shape(const spmm_args& a, int shape) {
     const int grouping = shape >> 1;
     if (sizeof(VT) == 8)
-        return grouping == 0 ? 1 : -1;  // FP64 is bound by the FP64 pipe: one value per lane
-    const int kp = kp_for(a.k);
-    const int widest = lanes_vec<VT>(a, kp);
-    switch (grouping) {
-    case 0:
-        return widest;
-    case 1:
-        return widest > 1 ? 1 : -1;
-    case 2:
-        return (kp == 32 && widest >= 4) ? 2 : -1;
-    default:
-        return -1;
-    }
+        return grouping == 0 ? 1 : -1;
+    const int v = lanes_vec<VT>(a, kp_for(a.k)) >> grouping;
+    return v >= 1 ? v : -1;
 }
 
 template <typename VT, bool DOT>
@@ -846,7 +841,14 @@ int mm_dispatch(const dimgpu_csr5* m, const VT* vals, const spmm_args& a, const 
     if (v < 0)
         v = lanes_for_shape<VT>(a, launch);  // a grouping these operands cannot use: the default one
     if constexpr (sizeof(VT) == 4) {
-        // f32 is issue-bound: vector lanes share the per-element work over two or four elements
+        // f32 is issue-bound: with V values per lane a group has KP / V lanes, each warp step serves
+        // 32 V / KP elements, and a tile takes KP / V * 16 steps instead of KP * 16
+        if (kp == 8 && v == 4)
+            return mm_dispatch_kp<VT, 8, 4, DOT>(m, vals, a, sc, launch, st);
+        if (kp == 8 && v == 2)
+            return mm_dispatch_kp<VT, 8, 2, DOT>(m, vals, a, sc, launch, st);
+        if (kp == 16 && v == 4)
+            return mm_dispatch_kp<VT, 16, 4, DOT>(m, vals, a, sc, launch, st);
         if (kp == 16 && v == 2)
             return mm_dispatch_kp<VT, 16, 2, DOT>(m, vals, a, sc, launch, st);
         if (kp == 32 && v == 4)
@@ -874,6 +876,12 @@ cudaError_t mm_attrs() {
     if ((e = mm_attr<VT, 32, 1, 8, 3, DOT>()) != cudaSuccess) return e;
     if ((e = mm_attr<VT, 32, 1, 16, 2, DOT>()) != cudaSuccess) return e;
     if constexpr (sizeof(VT) == 4) {
+        if ((e = mm_attr<VT, 8, 4, 8, 3, DOT>()) != cudaSuccess) return e;
+        if ((e = mm_attr<VT, 8, 4, 16, 2, DOT>()) != cudaSuccess) return e;
+        if ((e = mm_attr<VT, 8, 2, 8, 3, DOT>()) != cudaSuccess) return e;
+        if ((e = mm_attr<VT, 8, 2, 16, 2, DOT>()) != cudaSuccess) return e;
+        if ((e = mm_attr<VT, 16, 4, 8, 3, DOT>()) != cudaSuccess) return e;
+        if ((e = mm_attr<VT, 16, 4, 16, 2, DOT>()) != cudaSuccess) return e;
         if ((e = mm_attr<VT, 16, 2, 8, 3, DOT>()) != cudaSuccess) return e;
         if ((e = mm_attr<VT, 16, 2, 16, 2, DOT>()) != cudaSuccess) return e;
         if ((e = mm_attr<VT, 32, 4, 8, 3, DOT>()) != cudaSuccess) return e;

@@ -179,9 +179,10 @@ DIMGPU_API int dimgpu_csr5_spmm(const dimgpu_csr5* m, uint32_t k, const double* 
 DIMGPU_API int dimgpu_csr5_spmm_f32(const dimgpu_csr5* m, uint32_t k, const float* X, uint64_t ldx, float* Y,
                                     uint64_t ldy, void* stream);
 /* The shape the autotuner picked for (k, f32), -1 before the first call.  Bit 0 is the launch shape
- * (0: 8 warps x 3 stages, 1: 16 x 2); bits 1-2 the lane grouping (0: the widest vector lanes the operands
- * allow -- f32 lanes hold k/8 right-hand sides at k = 16, 32 --, 1: one right-hand side per lane, 2: two
- * per lane at k > 16).  No reference counterpart (the reference has no SpMM). */
+ * (0: 8 warps x 3 stages, 1: 16 x 2); bits 1-2 the lane grouping g: each lane holds w >> g right-hand
+ * sides, w being the widest the operands allow (f32: 4 or 2 when k and the leading dimensions are
+ * multiples of it and X, Y are aligned to it, else 1; FP64: 1), so g = 0 the widest, 1 half of it, 2 a
+ * quarter.  No reference counterpart (the reference has no SpMM). */
 DIMGPU_API int dimgpu_csr5_spmm_shape(const dimgpu_csr5* m, uint32_t k, int f32, int* shape);
 /* Pins the shape for (k, f32) (0..5; -1 re-tunes on the next call), e.g. for reproducible timings.  A
  * grouping the operands cannot use falls back to grouping 0 with the same launch shape. */
