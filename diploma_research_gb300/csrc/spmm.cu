@@ -4,21 +4,22 @@
 // by cp.async.bulk on an mbarrier ring, each warp owning a contiguous run of tiles, rows that cross runs
 // finished by a decoupled look-back, the CSR tail by the last CTA.
 //
-// Lanes.  KP = k rounded up to 8, 16 or 32.  Each lane holds V consecutive right-hand sides (f32: V = 4, 2
-// or 1, chosen by timing among those k and the leading dimensions allow with 16- or 8-byte vector
+// Lanes.  KP = k rounded up to 8, 16 or 32.  Each lane holds V consecutive right-hand sides (f32: V = 4,
+// 2 or 1, chosen by timing among those k and the leading dimensions allow with 16- or 8-byte vector
 // accesses; FP64: V = 1), so a lane group has LG = KP / V lanes and a warp G = 32 / LG groups; lane j of a
-// group holds right-hand
-// sides [j V, (j+1) V).  Group g walks the tile elements of tile columns [g LG, (g+1) LG) -- 16 LG consecutive
-// elements in CSR order -- one element per step: the element's value and column index come from shared
-// memory (16-byte loads of a whole tile column), every lane gathers X[col, jV .. jV+V) (one coalesced
-// k-wide row per group) and accumulates.  So one warp step does G elements x KP right-hand sides of
-// useful work: GB300's FP64 pipe (a warp-wide DFMA costs the same whatever the number of active lanes)
-// is kept full when k < 32, and with V > 1 the per-element overhead (flags, shared loads, shuffles), which
-// bounds the f32 product (it is issue-bound), is paid once for V right-hand sides: a tile takes 16 LG
-// warp steps.  A set bit_flag bit closes the group's running row
-// (written as one k-wide Y row); after the tile the groups' head and tail sums are joined in group order
-// with shuffles, which finishes the rows that span groups and yields the tile's head and open segments
-// for the in-order carry chain -- the same left-to-right sums as the SpMV.
+// group holds right-hand sides [j V, (j+1) V).  Group g walks the tile elements of tile columns
+// [g LG, (g+1) LG) -- 16 LG consecutive elements in CSR order -- one element per step: the element's value
+// and column index come from shared memory (16-byte loads of a whole tile column), every lane gathers
+// X[col, jV .. jV+V) (one coalesced k-wide row per group) and accumulates.  So one warp step does G
+// elements x KP right-hand sides of useful work: GB300's FP64 pipe (a warp-wide DFMA costs the same
+// whatever the number of active lanes) is kept full when k < 32, and with V > 1 the per-element overhead
+// (flags, shared loads, shuffles), which bounds the f32 product (it is issue-bound), is paid once for V
+// right-hand sides: a tile takes 16 LG warp steps.  A set bit_flag bit closes the group's running row
+// (written as one k-wide Y row); after the tile the groups' head and tail sums are joined with shuffles,
+// which finishes the rows that span groups and yields the tile's head and open segments for the in-order
+// carry chain: in group order when a warp has one or two groups (the SpMV's left-to-right sums), as a
+// log-step prefix over the groups' affine maps when it has four or more (a row spanning groups is then
+// summed in a tree order).
 //
 // The optional epilogue of the block CG computes, per right-hand side, dot_j = sum_i X[i,j] Y[i,j]
 // (products and per-tile partial sums in the value type, accumulated in f64 across tiles and CTAs in a
@@ -152,6 +153,15 @@ __device__ __forceinline__ vv<VT, V> vv_sum(const vv<VT, V>& x, const vv<VT, V>&
         r.a[i] = x.a[i] + y.a[i];
     return r;
 }
+template <typename VT, int V>
+__device__ __forceinline__ vv<VT, V> vv_shfl_up(const vv<VT, V>& x, unsigned d) {
+    vv<VT, V> r;
+#pragma unroll
+    for (int i = 0; i < V; ++i)
+        r.a[i] = __shfl_up_sync(kFull, x.a[i], d);
+    return r;
+}
+
 template <typename VT, int V>
 __device__ __forceinline__ vv<VT, V> vv_shfl(const vv<VT, V>& x, int src) {
     vv<VT, V> r;
@@ -409,6 +419,7 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
                 const uint32_t c0 = g * LG;
                 // segments are numbered by the row starts after tile element 0 (y_offset counts element 0 once)
                 uint32_t seg = (c0 == 0) ? 0u : ((sd[c0] & G::YMASK) - 1u);
+                const uint32_t seg0 = seg;  // the segment open when the group begins
                 W acc = vv_zero<VT, V>(), head = vv_zero<VT, V>();
                 bool hs = false;
                 // gathers of rows [r0, r0 + RB) of tile column c (X[col, jV .. jV+V) per element)
@@ -468,33 +479,70 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
                 if (!hs)
                     head = acc;
 
-                // ---- join the groups in order: rows spanning groups, the tile's head and open segments ----
-                W open_v = vv_zero<VT, V>(), H = vv_zero<VT, V>();
+                // ---- join the groups: rows spanning groups, the tile's head and open segments ----
+                W H, Lt;
                 uint32_t open_seg = 0;
-                bool closed0 = false;
+                if constexpr (NG >= 4) {
+                    // The partial R of the row open when group g begins follows R_{g+1} = f_g(R_g), with
+                    // f_g(R) = hs_g ? acc_g : R + head_g (a group with a row start hands on its tail, one
+                    // without adds its sum).  The prefixes of the maps f_g o ... o f_0 over the groups take
+                    // log2(NG) shuffle steps (Hillis-Steele) instead of NG in turn; every group with a row
+                    // start then closes its row, R_g + head_g, at once.
+                    bool keep = !hs;             // f_g keeps R
+                    W c = hs ? acc : head;       // and adds c
     #pragma unroll
-                for (int gg = 0; gg < NG; ++gg) {
-                    const int src = gg * LG + (int)j;
-                    const uint32_t ghs = __shfl_sync(kFull, hs ? 1u : 0u, src);
-                    const W ghd = vv_shfl<VT, V>(head, src);
-                    const W gtl = vv_shfl<VT, V>(acc, src);
-                    const uint32_t gseg = __shfl_sync(kFull, seg, src);
-                    vv_add<VT, V>(open_v, ghd);
-                    if (ghs) {
-                        if (open_seg == 0) {
-                            H = open_v;
-                            closed0 = true;
-                        } else {
-                            put_row(g == (unsigned)gg, row_of(open_seg), open_v);
+                    for (unsigned d = 1; d < (unsigned)NG; d <<= 1) {
+                        const bool keep_p = __shfl_up_sync(kFull, keep ? 1u : 0u, d * LG) != 0u;
+                        const W c_p = vv_shfl_up<VT, V>(c, d * LG);
+                        if (g >= d) {
+                            if (keep)
+                                vv_add<VT, V>(c, c_p);
+                            keep = keep && keep_p;
                         }
-                        open_v = gtl;
-                        open_seg = gseg;
                     }
+                    W R = vv_shfl_up<VT, V>(c, LG);  // the prefix of the groups before g, applied to 0
+                    if (g == 0)
+                        R = vv_zero<VT, V>();
+                    const W closed = vv_sum<VT, V>(R, head);
+                    const uint32_t starts = __ballot_sync(kFull, hs);  // LG bits per group with a row start
+                    Lt = vv_shfl<VT, V>(c, (NG - 1) * LG + (int)j);
+                    if (starts) {
+                        const int first = (int)((__ffs(starts) - 1) / LG), last = (int)((31 - __clz(starts)) / LG);
+                        // the first row start closes the tile's head segment (segment 0, for the carry chain)
+                        put_row(hs && g != (unsigned)first, row_of(seg0), closed);
+                        H = vv_shfl<VT, V>(closed, first * LG + (int)j);
+                        open_seg = __shfl_sync(kFull, seg, last * LG + (int)j);
+                    } else {
+                        H = Lt;
+                    }
+                } else {
+                    W open_v = vv_zero<VT, V>();
+                    H = vv_zero<VT, V>();
+                    bool closed0 = false;
+    #pragma unroll
+                    for (int gg = 0; gg < NG; ++gg) {
+                        const int src = gg * LG + (int)j;
+                        const uint32_t ghs = __shfl_sync(kFull, hs ? 1u : 0u, src);
+                        const W ghd = vv_shfl<VT, V>(head, src);
+                        const W gtl = vv_shfl<VT, V>(acc, src);
+                        const uint32_t gseg = __shfl_sync(kFull, seg, src);
+                        vv_add<VT, V>(open_v, ghd);
+                        if (ghs) {
+                            if (open_seg == 0) {
+                                H = open_v;
+                                closed0 = true;
+                            } else {
+                                put_row(g == (unsigned)gg, row_of(open_seg), open_v);
+                            }
+                            open_v = gtl;
+                            open_seg = gseg;
+                        }
+                    }
+                    if (!closed0)
+                        H = open_v;
+                    Lt = open_v;
                 }
-                if (!closed0)
-                    H = open_v;
                 const uint32_t K = open_seg + 1;
-                const W Lt = open_v;
                 const uint32_t row_last = (K == 1) ? row_start : row_of(open_seg);
 
                 // ---- in-order carry chain over the warp's tiles (per right-hand side, same in every group) ----
