@@ -243,6 +243,10 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
     using W = vv<VT, V>;
     constexpr int LG = KP / V;   // lanes per group
     constexpr int NG = 32 / LG;  // lane groups per warp
+    // The plain f32 product with vector lanes is issue-bound: its walk closes rows with selects and a
+    // predicated store (one instruction stream for every group).  FP64 (bound by the FP64 pipe), one value
+    // per lane and the dot epilogue (registers) keep the branch, which costs fewer instructions per step.
+    constexpr bool kSelectWalk = sizeof(VT) == 4 && V > 1 && !DOT;
     // rows gathered together (registers: RB x V values of x in flight per lane)
     constexpr int RB = (V * sizeof(VT) <= 8) ? kSigma : kSigma * 8 / (int)(V * sizeof(VT));
     extern __shared__ __align__(128) unsigned char smem[];
@@ -439,18 +443,32 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
                     stage_vals<VT>(st, c, v);
     #pragma unroll
                     for (int r = 0; r < RB; ++r) {
-                        if ((fl >> (r0 + r)) & 1u) {
-                            if (hs)
-                                put_row(true, row_of(seg), acc);  // a row that began in this group's range
-                            else
-                                head = acc;
-                            hs = true;
-                            ++seg;
-                            acc = vv_zero<VT, V>();
-                        }
+                        // a row start: the running row closes (written when it began in this group's range,
+                        // else kept as the group's head)
+                        const bool bit = ((fl >> (r0 + r)) & 1u) != 0;
+                        if constexpr (kSelectWalk) {
+                            put_row(bit && hs, row_of(seg), acc);
     #pragma unroll
-                        for (int q = 0; q < V; ++q)
-                            acc.a[q] = fma(v[r0 + r], x[r].a[q], acc.a[q]);
+                            for (int q = 0; q < V; ++q) {
+                                head.a[q] = (bit && !hs) ? acc.a[q] : head.a[q];
+                                acc.a[q] = fma(v[r0 + r], x[r].a[q], bit ? VT(0) : acc.a[q]);
+                            }
+                            seg += bit ? 1u : 0u;
+                            hs = hs || bit;
+                        } else {
+                            if (bit) {
+                                if (hs)
+                                    put_row(true, row_of(seg), acc);  // a row that began in this group's range
+                                else
+                                    head = acc;
+                                hs = true;
+                                ++seg;
+                                acc = vv_zero<VT, V>();
+                            }
+    #pragma unroll
+                            for (int q = 0; q < V; ++q)
+                                acc.a[q] = fma(v[r0 + r], x[r].a[q], acc.a[q]);
+                        }
                     }
                 };
                 if constexpr (sizeof(VT) == 4 && V == 1) {
