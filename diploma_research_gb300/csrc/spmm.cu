@@ -243,10 +243,10 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
     using W = vv<VT, V>;
     constexpr int LG = KP / V;   // lanes per group
     constexpr int NG = 32 / LG;  // lane groups per warp
-    // The plain f32 product with vector lanes is issue-bound: its walk closes rows with selects and a
-    // predicated store (one instruction stream for every group).  FP64 (bound by the FP64 pipe), one value
-    // per lane and the dot epilogue (registers) keep the branch, which costs fewer instructions per step.
-    constexpr bool kSelectWalk = sizeof(VT) == 4 && V > 1 && !DOT;
+    // The f32 product with vector lanes is issue-bound: its walk closes rows with selects and a predicated
+    // store (one instruction stream for every group).  FP64 (bound by the FP64 pipe) and one value per lane
+    // keep the branch, which costs fewer instructions per step there.
+    constexpr bool kSelectWalk = sizeof(VT) == 4 && V > 1;
     // rows gathered together (registers: RB x V values of x in flight per lane)
     constexpr int RB = (V * sizeof(VT) <= 8) ? kSigma : kSigma * 8 / (int)(V * sizeof(VT));
     extern __shared__ __align__(128) unsigned char smem[];
@@ -290,14 +290,14 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
     // dot epilogue: READBACK -- the rows this warp wrote in the current tile, read back after it; else the
     // tile's products, taken at each row write
     constexpr bool READBACK = NG > 1;
-    uint32_t wr_lo = 0xFFFFFFFFu, wr_hi = 0u;
     W tdot = vv_zero<VT, V>();
     const bool no_empty = p.n_empty == 0;
     bool open = false, cal_valid = false;
     W carry = vv_zero<VT, V>(), cal = vv_zero<VT, V>();
     uint32_t carry_row = 0, cal_row = 0;
 
-    // k-wide row write by the lanes of one group (`mine`), remembered or with its share of the dot
+    // k-wide row write by the lanes of one group (`mine`), with its share of the dot when it is taken at
+    // the write
     auto put_row = [&](bool mine, uint32_t row, const W& val) {
         if (mine) {
             if (active) {
@@ -308,10 +308,6 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
                     for (int q = 0; q < V; ++q)
                         tdot.a[q] = fma(val.a[q], xr.a[q], tdot.a[q]);
                 }
-            }
-            if constexpr (DOT && READBACK) {
-                wr_lo = min(wr_lo, row);
-                wr_hi = max(wr_hi, row);
             }
         }
     };
@@ -328,8 +324,7 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
         }
     };
     // x.y over the rows [lo, hi] one tile finished, four rows per group in flight, summed in the value type
-    // and folded into dot_acc.  Every non-empty row of the range was written by this warp in this tile:
-    // the rows between two rows the tile wrote have all their elements in it.
+    // and folded into dot_acc.  Every non-empty row of the range was written by this warp in this tile.
     auto dot_rows = [&](uint32_t lo, uint32_t hi) {
         W ts = vv_zero<VT, V>();
 #pragma unroll 1
@@ -564,6 +559,8 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
                 const uint32_t row_last = (K == 1) ? row_start : row_of(open_seg);
 
                 // ---- in-order carry chain over the warp's tiles (per right-hand side, same in every group) ----
+                const bool open_prev = open;
+                const uint32_t carry_prev = carry_row;
                 if (K == 1) {
                     if (capped) {
                         if (open)
@@ -595,9 +592,17 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
                     carry_row = row_last;
                 }
                 if constexpr (DOT && READBACK) {
-                    const uint32_t lo = __reduce_min_sync(kFull, wr_lo), hi = __reduce_max_sync(kFull, wr_hi);
-                    wr_lo = 0xFFFFFFFFu;
-                    wr_hi = 0u;
+                    // The rows this tile wrote, a range known from the tile alone: the previous tile's open
+                    // row when this tile closed it (a capped tile, or one with a row start, after an open
+                    // row), the head row unless it went to the chunk's look-back, and every row between it
+                    // and the row left open at the end (the rows in between are closed here or empty).
+                    uint32_t lo = 0xFFFFFFFFu, hi = 0u;
+                    if (K > 1) {
+                        lo = (capped && open_prev) ? carry_prev : ((capped || open_prev) ? row_start : row_start + 1u);
+                        hi = row_last - 1u;
+                    } else if (capped && open_prev) {
+                        lo = hi = carry_prev;
+                    }
                     __syncwarp();  // the rows' stores by the other lanes are visible to the loads below
                     if (lo <= hi)
                         dot_rows(lo, hi);
