@@ -431,7 +431,10 @@ void write_file(const std::string& path, const node& root) {
 
 class inflater {
 public:
-    inflater(const uint8_t* in, size_t n, std::vector<uint8_t>& out) : in_(in), n_(n), out_(out) {}
+    // `limit`: the most bytes the stream may produce (a chunk's size); a stream that would produce more is
+    // not a chunk of this dataset
+    inflater(const uint8_t* in, size_t n, std::vector<uint8_t>& out, size_t limit)
+        : in_(in), n_(n), out_(out), limit_(limit) {}
 
     void run() {
         if (n_ < 2)
@@ -517,6 +520,7 @@ private:
         pos_ += 4;
         if ((uint16_t)~nlen != len || pos_ + len > n_)
             throw format_error("deflate chunk: bad stored block");
+        room(len);
         out_.insert(out_.end(), in_ + pos_, in_ + pos_ + len);
         pos_ += len;
     }
@@ -533,6 +537,7 @@ private:
         for (;;) {
             int s = decode(lit);
             if (s < 256) {
+                room(1);
                 out_.push_back((uint8_t)s);
             } else if (s == 256) {
                 return;
@@ -548,6 +553,7 @@ private:
                 if (back > out_.size())
                     throw format_error("deflate chunk: distance before the start");
                 const size_t from = out_.size() - back;
+                room(len);
                 for (uint32_t k = 0; k < len; ++k)
                     out_.push_back(out_[from + k]);
             }
@@ -615,11 +621,17 @@ private:
         codes(lit, dist);
     }
 
+    void room(size_t more) const {
+        if (out_.size() + more > limit_)
+            throw format_error("deflate chunk: expands past the chunk's size");
+    }
+
     const uint8_t* in_;
     size_t n_, pos_ = 0;
     uint32_t buf_ = 0;
     int cnt_ = 0;
     std::vector<uint8_t>& out_;
+    size_t limit_;
 };
 
 // ------------------------------------------------------------------------------------------------
@@ -1071,7 +1083,7 @@ private:
             if (deflate && !(fmask & 1)) {
                 std::vector<uint8_t> plain;
                 plain.reserve(chunk_elems * esz);
-                inflater(raw, csize, plain).run();
+                inflater(raw, csize, plain, chunk_elems * esz).run();
                 if (plain.size() < n)
                     throw format_error("deflate chunk shorter than its elements");
                 std::memcpy(out.data() + off0 * esz, plain.data(), n);

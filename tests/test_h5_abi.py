@@ -288,3 +288,18 @@ def test_wide_indices_are_narrowed_or_refused(native, tmp_path):
     rp, ci, v = np.zeros(61, np.uint32), np.zeros(m.nnz, np.uint32), np.zeros(m.nnz)
     rc = native.dimgpu_h5_read_matlab_compatible(_b(p), b"A", rp.ctypes.data, ci.ctypes.data, v.ctypes.data)
     assert rc == N.ERR_IO and b"32 bits" in native.dimgpu_last_error_string()
+
+
+def test_reader_refuses_a_chunk_that_inflates_past_its_size(native, tmp_path, monkeypatch):
+    """A deflate stream longer than its chunk (here: the chunk's bytes twice) is an error, not a buffer
+    that grows without bound."""
+    y = np.arange(300, dtype=np.float64)
+    p = tmp_path / "long.h5"
+    monkeypatch.setattr(h5, "_write_dataset", _chunked_writer(chunk=64, compress=lambda raw: zlib.compress(raw + raw)))
+    h5.write_vector(p, "Y", y)
+    monkeypatch.undo()
+    n = ctypes.c_uint64()
+    assert native.dimgpu_h5_vector_length(_b(p), b"Y", ctypes.byref(n)) == N.OK and n.value == 300
+    out = np.zeros(300)
+    assert native.dimgpu_h5_read_vector(_b(p), b"Y", out.ctypes.data) == N.ERR_IO
+    assert b"expands past" in native.dimgpu_last_error_string()
