@@ -1,8 +1,8 @@
 // h5.cpp -- the reference's HDF5 matrix files without libhdf5, behind the C ABI (dimgpu_h5_*).
 //
-// The reference keeps matrices in HDF5 through libhdf5 (include/dim/io/h5.h:62-115,
+// The reference keeps matrices in HDF5 through libhdf5 (include/dim/io/h5.h:68-115,
 // libs/dim/io/h5.cpp:12-74):
-//   * a MATLAB-compatible CSR group (write_matlab_compatible / read_matlab_compatible, h5.h:62-90):
+//   * a MATLAB-compatible CSR group (write_matlab_compatible / read_matlab_compatible, h5.h:68-97):
 //     datasets `data` (f64), `ir` (u32 column indices), `jc` (u32 row offsets) and the scalar u32
 //     attribute `MATLAB_sparse` = column count;
 //   * a CSR5 group (store / load_csr5, h5.cpp:45-74): the attribute `column_count` and the datasets

@@ -3,7 +3,7 @@
 The reference stores matrices with libhdf5 (libs/dim/io/h5.cpp, include/dim/io/h5.h):
 
 * a MATLAB-compatible CSR group (``write_matlab_compatible`` / ``read_matlab_compatible``,
-  include/dim/io/h5.h:62-90): datasets ``data`` (f64), ``ir`` (u32 column indices), ``jc`` (u32 row
+  include/dim/io/h5.h:68-97): datasets ``data`` (f64), ``ir`` (u32 column indices), ``jc`` (u32 row
   offsets) and the scalar u32 attribute ``MATLAB_sparse`` = column count;
 * a CSR5 group (``store`` / ``load_csr5``, libs/dim/io/h5.cpp:45-74): attribute ``column_count`` and
   datasets ``vals``, ``col_idx``, ``row_ptr``, ``tile_ptr``, ``tile_desc`` (one H5T array of 4 u32 per
@@ -630,7 +630,7 @@ class H5Writer:
 
 
 def write_matlab_compatible(path, group: str, m, append: bool = False):
-    """include/dim/io/h5.h:62-70: data, ir (column indices), jc (row offsets), MATLAB_sparse = cols."""
+    """include/dim/io/h5.h:68-76: data, ir (column indices), jc (row offsets), MATLAB_sparse = cols."""
     with H5Writer(path, append=append) as w:
         w.remove(group)
         w.dataset(f"{group}/data", np.asarray(m.values, np.float64))
@@ -640,7 +640,7 @@ def write_matlab_compatible(path, group: str, m, append: bool = False):
 
 
 def read_matlab_compatible(path, group: str = "A"):
-    """include/dim/io/h5.h:72-90."""
+    """include/dim/io/h5.h:78-97."""
     from ..mat import csr, dimensions_t
 
     with H5Reader(path) as r:

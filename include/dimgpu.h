@@ -279,7 +279,7 @@ DIMGPU_API int dimgpu_cg_adjoint(const dimgpu_csr5* m, const double* g, const do
 /* ---- diagnostics ------------------------------------------------------------------------------ */
 
 /* ---- HDF5 matrix files ------------------------------------------------------------------------
- * The reference's dim::io::h5 (include/dim/io/h5.h:62-115, libs/dim/io/h5.cpp:45-74) on files it
+ * The reference's dim::io::h5 (include/dim/io/h5.h:68-115, libs/dim/io/h5.cpp:45-74) on files it
  * writes with libhdf5, without libhdf5: the library reads and writes the part of the HDF5 format those
  * files use (superblock 0/1, version-1 object headers, symbol-table groups, contiguous, compact and
  * chunked 1-D datasets, the deflate filter; files written with libver "latest" are refused) and writes
@@ -287,7 +287,7 @@ DIMGPU_API int dimgpu_cg_adjoint(const dimgpu_csr5* m, const double* g, const do
  * be read or written or lies outside that subset.  A writer with append != 0 keeps the other members
  * of an existing file (it is read, then rewritten through a temporary file). */
 
-/* read_matlab_compatible (h5.h:72-90), first call: the sizes of the MATLAB-compatible CSR group
+/* read_matlab_compatible (h5.h:78-97), first call: the sizes of the MATLAB-compatible CSR group
  * `group` (datasets data, ir, jc; attribute MATLAB_sparse = column count). */
 DIMGPU_API int dimgpu_h5_csr_dimensions(const char* path, const char* group, uint32_t* rows, uint32_t* cols,
                                         uint64_t* nnz);
@@ -295,7 +295,7 @@ DIMGPU_API int dimgpu_h5_csr_dimensions(const char* path, const char* group, uin
  * caller buffers; indices stored in wider integer types are narrowed to u32 (an error if one does not fit). */
 DIMGPU_API int dimgpu_h5_read_matlab_compatible(const char* path, const char* group, uint32_t* row_ptr,
                                                 uint32_t* col_indices, double* values);
-/* write_matlab_compatible (h5.h:62-70): replaces `group` (the whole file unless append). */
+/* write_matlab_compatible (h5.h:68-76): replaces `group` (the whole file unless append). */
 DIMGPU_API int dimgpu_h5_write_matlab_compatible(const char* path, const char* group, uint32_t rows, uint32_t cols,
                                                  uint64_t nnz, const uint32_t* row_ptr, const uint32_t* col_indices,
                                                  const double* values, int append);

@@ -14,7 +14,7 @@
 //   the dim_sp CG loop                                 dim::gpu::cg_solver
 //   dim::io::h5::read_matlab_compatible,               dim::gpu::io::read_matlab_compatible,
 //     write_matlab_compatible, load_csr5, store          write_matlab_compatible, load_csr5, store
-//     (include/dim/io/h5.h:62-115)                       (HDF5 files without libhdf5; see dimgpu.h)
+//     (include/dim/io/h5.h:68-115)                       (HDF5 files without libhdf5; see dimgpu.h)
 //
 // from_csr takes any matrix type with the members of dim::mat::csr<double> (csr.h:19-40):
 // `dimensions.rows`, `dimensions.cols`, and contiguous `values`, `row_start_offsets` (u32) and
@@ -227,7 +227,7 @@ private:
     size_t rows_{};
 };
 
-// The reference's HDF5 matrix IO (dim::io::h5, include/dim/io/h5.h:62-115; libs/dim/io/h5.cpp:45-74).
+// The reference's HDF5 matrix IO (dim::io::h5, include/dim/io/h5.h:68-115; libs/dim/io/h5.cpp:45-74).
 // File errors throw dim::gpu::error with DIMGPU_ERR_IO, a missing group std::invalid_argument.
 namespace io {
 
@@ -239,7 +239,7 @@ struct csr_matrix {
     std::vector<uint32_t> col_indices;
 };
 
-// read_matlab_compatible (h5.h:72-90): datasets data, ir, jc and the attribute MATLAB_sparse.
+// read_matlab_compatible (h5.h:78-97): datasets data, ir, jc and the attribute MATLAB_sparse.
 inline csr_matrix read_matlab_compatible(const std::string& path, const std::string& group = "A") {
     uint32_t rows = 0, cols = 0;
     uint64_t nnz = 0;
@@ -251,7 +251,7 @@ inline csr_matrix read_matlab_compatible(const std::string& path, const std::str
     return m;
 }
 
-// write_matlab_compatible (h5.h:62-70) of any matrix with the members of dim::mat::csr<double>.
+// write_matlab_compatible (h5.h:68-76) of any matrix with the members of dim::mat::csr<double>.
 template <typename Csr>
 void write_matlab_compatible(const std::string& path, const std::string& group, const Csr& m, bool append = false) {
     const auto nnz = static_cast<uint64_t>(std::size(m.values));
