@@ -98,3 +98,43 @@ def test_spmm_matches_spmv_columns(native, torch_cuda):
         A.spmv(X[:, j].contiguous(), y)
         torch.cuda.synchronize()
         assert torch.allclose(Y[:, j], y, rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("f32", [True, False])
+@pytest.mark.parametrize("ldx,ldy,offset", [(10, 11, 0), (9, 8, 0), (8, 8, 1), (12, 16, 2)])
+def test_spmm_strided_and_unaligned_operands(native, torch_cuda, f32, ldx, ldy, offset):
+    """k = 8 right-hand sides in wider row-major buffers (leading dimensions ldx, ldy) starting `offset`
+    elements into them: the lane widths the operands do not allow (vector accesses need k, both leading
+    dimensions and both base addresses to fit them) fall back to narrower lanes; every shape, pinned,
+    gives the product."""
+    import ctypes
+
+    from diploma_research_gb300 import _native as N
+
+    torch = torch_cuda
+    k = 8
+    rng = np.random.default_rng(ldx * 100 + ldy * 10 + offset)
+    m = random_csr(rng, 3000, 2500, 8.0, empty_frac=0.05, long_rows=2, long_len=(600, 2000))
+    A = csr5.from_csr(m)
+    dt, npdt = (torch.float32, np.float32) if f32 else (torch.float64, np.float64)
+    X = rng.uniform(-1, 1, (m.dimensions.cols, k)).astype(npdt)
+    Xb = torch.zeros((m.dimensions.cols * ldx + offset + ldx,), device="cuda", dtype=dt)
+    Xb[offset:offset + m.dimensions.cols * ldx].view(m.dimensions.cols, ldx)[:, :k] = torch.tensor(X, device="cuda")
+    Yb = torch.full((m.dimensions.rows * ldy + offset + ldy,), float("nan"), device="cuda", dtype=dt)
+    esz = 4 if f32 else 8
+    fn = native.dimgpu_csr5_spmm_f32 if f32 else native.dimgpu_csr5_spmm
+    S = m.to_scipy()
+    if f32:
+        S.data = S.data.astype(np.float32).astype(np.float64)
+    Xe = X.astype(np.float64)
+    Y_ref = S @ Xe
+    bound = (_f32_bound(m, abs(S) @ np.abs(Xe)) if f32 else 1e-12 * (abs(S) @ np.abs(Xe))) + 1e-300
+    for shape in range(6):
+        set_spmm_shape(A, k, shape, f32)
+        Yb.fill_(float("nan"))
+        rc = fn(A._h, k, Xb.data_ptr() + offset * esz, ldx, Yb.data_ptr() + offset * esz, ldy, None)
+        assert rc == N.OK, native.dimgpu_last_error_string()
+        torch.cuda.synchronize()
+        Y = Yb[offset:offset + m.dimensions.rows * ldy].view(m.dimensions.rows, ldy)[:, :k].cpu().numpy()
+        err = np.abs(Y.astype(np.float64) - Y_ref)
+        assert np.all(err <= bound), (shape, float(np.max(err / bound)))
