@@ -143,6 +143,8 @@ _SIGNATURES = {
     "dimgpu_h5_vector_length": [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_u64)],
     "dimgpu_h5_read_vector": [ctypes.c_char_p, ctypes.c_char_p, _vp],
     "dimgpu_h5_write_vector": [ctypes.c_char_p, ctypes.c_char_p, _u64, _vp, ctypes.c_int],
+    "dimgpu_mm_csr_dimensions": [ctypes.c_char_p, ctypes.POINTER(_u32), ctypes.POINTER(_u32), ctypes.POINTER(_u64)],
+    "dimgpu_mm_read_csr": [ctypes.c_char_p, _vp, _vp, _vp],
 }
 
 

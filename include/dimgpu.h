@@ -315,6 +315,18 @@ DIMGPU_API int dimgpu_h5_read_vector(const char* path, const char* dataset, doub
 DIMGPU_API int dimgpu_h5_write_vector(const char* path, const char* dataset, uint64_t n, const double* y,
                                       int overwrite);
 
+/* ---- Matrix Market files ----------------------------------------------------------------------
+ * dim::io::matrix_market::load_as_csr (include/dim/io/matrix_market.h:25-83) without scnlib: a coordinate
+ * file (real, integer or pattern -- pattern entries get 1.0; general, symmetric or Hermitian) to CSR the
+ * way csr::from_coo builds it (csr.h:42-77): entries in file order, each off-diagonal entry of a symmetric
+ * file followed by its mirror (coo.h:33-46), rows sorted by column (stable: equal columns keep file order).
+ * First call: the sizes (nnz after the symmetric expansion); second call: the arrays into caller buffers
+ * (row_ptr rows + 1, col_indices and values nnz each).  Each call reads the file.  DIMGPU_ERR_INVALID_ARGUMENT
+ * for a file that is not a coordinate Matrix Market matrix or whose entries do not scan or lie outside
+ * the matrix; DIMGPU_ERR_IO when it cannot be read. */
+DIMGPU_API int dimgpu_mm_csr_dimensions(const char* path, uint32_t* rows, uint32_t* cols, uint64_t* nnz);
+DIMGPU_API int dimgpu_mm_read_csr(const char* path, uint32_t* row_ptr, uint32_t* col_indices, double* values);
+
 DIMGPU_API const char* dimgpu_last_error_string(void);
 /* ABI version of this library (2: status queries, SpMM shapes with lane grouping, no persistent CG engine). */
 DIMGPU_API int dimgpu_version(void);

@@ -15,6 +15,7 @@
 //   dim::io::h5::read_matlab_compatible,               dim::gpu::io::read_matlab_compatible,
 //     write_matlab_compatible, load_csr5, store          write_matlab_compatible, load_csr5, store
 //     (include/dim/io/h5.h:68-115)                       (HDF5 files without libhdf5; see dimgpu.h)
+//   dim::io::matrix_market::load_as_csr                dim::gpu::io::load_matrix_market (no scnlib)
 //
 // from_csr takes any matrix type with the members of dim::mat::csr<double> (csr.h:19-40):
 // `dimensions.rows`, `dimensions.cols`, and contiguous `values`, `row_start_offsets` (u32) and
@@ -288,6 +289,17 @@ inline std::vector<double> read_vector(const std::string& path, const std::strin
 inline void write_vector(const std::string& path, const std::string& dataset, std::span<const double> y,
                          bool overwrite = false) {
     check(dimgpu_h5_write_vector(path.c_str(), dataset.c_str(), y.size(), y.data(), overwrite ? 1 : 0));
+}
+
+// dim::io::matrix_market::load_as_csr (matrix_market.h:25-83): a coordinate Matrix Market file as CSR.
+inline csr_matrix load_matrix_market(const std::string& path) {
+    uint32_t rows = 0, cols = 0;
+    uint64_t nnz = 0;
+    check(dimgpu_mm_csr_dimensions(path.c_str(), &rows, &cols, &nnz));
+    csr_matrix m{{rows, cols}, std::vector<double>(nnz), std::vector<uint32_t>(size_t(rows) + 1),
+                 std::vector<uint32_t>(nnz)};
+    check(dimgpu_mm_read_csr(path.c_str(), m.row_start_offsets.data(), m.col_indices.data(), m.values.data()));
+    return m;
 }
 
 }  // namespace io

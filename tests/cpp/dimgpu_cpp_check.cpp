@@ -1,7 +1,7 @@
 // A C++ caller of dimgpu through include/dimgpu.hpp, as a dim user would write it: from_csr, spmv on
 // host spans and on device memory (CUDA runtime allocations, a stream, the status query), the CG
-// solver, the reference's exceptions, and the HDF5 matrix IO (write_matlab_compatible and
-// read_matlab_compatible, store and load_csr5, the result vector).
+// solver, the reference's exceptions, and the file IO (HDF5: write_matlab_compatible and
+// read_matlab_compatible, store and load_csr5, the result vector; Matrix Market: load_matrix_market).
 //
 //   dimgpu_cpp_check <output file>
 //
@@ -133,6 +133,18 @@ int main(int argc, char** argv) {
     std::vector<double> y5(n);
     L.spmv(x, y5);
     EXPECT(y5 == y);  // the same matrix, the same kernel: the same bits
+    // the same matrix through a Matrix Market file (written here, general coordinate form)
+    const std::string mtxpath = std::string(argv[1]) + ".mtx";
+    FILE* mf = std::fopen(mtxpath.c_str(), "w");
+    EXPECT(mf != nullptr);
+    std::fprintf(mf, "%%%%MatrixMarket matrix coordinate real general\n%% written by the check\n%u %u %zu\n", n, n,
+                 v.size());
+    for (uint32_t r = 0; r < n; ++r)
+        for (uint32_t e = rp[r]; e < rp[r + 1]; ++e)
+            std::fprintf(mf, "%u %u %.17g\n", r + 1, ci[e] + 1, v[e]);
+    std::fclose(mf);
+    const dim::gpu::io::csr_matrix mmx = dim::gpu::io::load_matrix_market(mtxpath);
+    EXPECT(mmx.values == v && mmx.row_start_offsets == rp && mmx.col_indices == ci);
     dim::gpu::io::write_vector(h5path, "z", z);
     EXPECT(dim::gpu::io::read_vector(h5path, "z") == z);
     threw = false;
