@@ -55,11 +55,15 @@ def test_spmm_random(native, torch_cuda, k):
     _check(torch_cuda, m, k, seed=k)
 
 
-@pytest.mark.parametrize("k", [8, 32])
+@pytest.mark.parametrize("k", [2, 6, 8, 12, 20, 28, 32])
 def test_spmm_f32(native, torch_cuda, k):
+    """f32 at widths where the vector lanes leave lanes of a group idle (k = 2, 6: two values per lane;
+    12, 20, 28: four) and where they fill it; the autotuned shape, then every shape pinned."""
     rng = np.random.default_rng(100 + k)
     m = random_csr(rng, 3000, 3000, 9.0, empty_frac=0.05, long_rows=2, long_len=(600, 2000))
-    _check(torch_cuda, m, k, seed=k, f32=True)
+    A = _check(torch_cuda, m, k, seed=k, f32=True)
+    for shape in range(6):
+        _check(torch_cuda, m, k, seed=k + shape, f32=True, A=A, shape=shape)
 
 
 @pytest.mark.parametrize("f32", [False, True])
