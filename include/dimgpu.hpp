@@ -12,6 +12,8 @@
 //   csr5::create_calibrator() (csr5.h:809)             csr5::create_calibrator()
 //   csr5::tail_partition_start(), non_zero_count()     the same names
 //   the dim_sp CG loop                                 dim::gpu::cg_solver
+//   (no counterpart: batching, differentiation)        csr5::spmm_device, block_cg_solver,
+//                                                        csr5::spmv_transpose_device, cg_adjoint
 //   dim::io::h5::read_matlab_compatible,               dim::gpu::io::read_matlab_compatible,
 //     write_matlab_compatible, load_csr5, store          write_matlab_compatible, load_csr5, store
 //     (include/dim/io/h5.h:68-115)                       (HDF5 files without libhdf5; see dimgpu.h)
@@ -156,6 +158,20 @@ public:
         return r;
     }
 
+    // Y := A X for k right-hand sides (device memory, row-major, leading dimensions ldx, ldy >= k); the
+    // first call for a (k, precision) times the candidate shapes (not inside a stream capture).
+    void spmm_device(uint32_t k, const double* X, uint64_t ldx, double* Y, uint64_t ldy, void* stream = nullptr) const {
+        check(dimgpu_csr5_spmm(h_, k, X, ldx, Y, ldy, stream));
+    }
+    void spmm_device(uint32_t k, const float* X, uint64_t ldx, float* Y, uint64_t ldy, void* stream = nullptr) const {
+        check(dimgpu_csr5_spmm_f32(h_, k, X, ldx, Y, ldy, stream));
+    }
+
+    // y := A^T x on device memory (x: rows, y: cols).
+    void spmv_transpose_device(const double* x, double* y, void* stream = nullptr) const {
+        check(dimgpu_csr5_spmv_transpose(h_, x, y, stream));
+    }
+
     calibrator create_calibrator() const {
         dimgpu_calibrator* c = nullptr;
         check(dimgpu_calibrator_create(h_, &c));
@@ -227,6 +243,65 @@ private:
     dimgpu_cg_solver* h_{};
     size_t rows_{};
 };
+
+// k simultaneous CG solves sharing one SpMM per iteration, each column with its own convergence (the
+// dim_sp recurrence per column).  The matrix must outlive the solver.
+class block_cg_solver {
+public:
+    block_cg_solver(const csr5& a, uint32_t k, const dimgpu_cg_params& params, void* stream = nullptr) : k_(k) {
+        check(dimgpu_block_cg_create(a.handle(), k, &params, stream, &h_));
+    }
+    block_cg_solver(const block_cg_solver&) = delete;
+    block_cg_solver& operator=(const block_cg_solver&) = delete;
+    block_cg_solver(block_cg_solver&& o) noexcept : h_(std::exchange(o.h_, nullptr)), k_(o.k_) {}
+    block_cg_solver& operator=(block_cg_solver&& o) noexcept {
+        if (this != &o) {
+            reset();
+            h_ = std::exchange(o.h_, nullptr);
+            k_ = o.k_;
+        }
+        return *this;
+    }
+    ~block_cg_solver() { reset(); }
+
+    // B and X (initial guesses, overwritten by the solutions): n x k row-major device blocks.  Per-column
+    // iteration counts and true relative residuals go to `col_iterations` / `col_rel_residual` when
+    // given (k entries each).  A column that stops at max_it makes it throw dim::gpu::error
+    // (DIMGPU_ERR_NOT_CONVERGED) unless `throw_on_failure` is false.
+    dimgpu_block_cg_stats solve_device(const double* B, uint64_t ldb, double* X, uint64_t ldx,
+                                       std::span<int64_t> col_iterations = {}, std::span<double> col_rel_residual = {},
+                                       void* stream = nullptr, bool throw_on_failure = true) {
+        if ((!col_iterations.empty() && col_iterations.size() != k_) ||
+            (!col_rel_residual.empty() && col_rel_residual.size() != k_))
+            throw std::invalid_argument("per-column outputs must have k entries");
+        dimgpu_block_cg_stats st{};
+        const int rc = dimgpu_block_cg_solve(h_, B, ldb, X, ldx, &st,
+                                             col_iterations.empty() ? nullptr : col_iterations.data(),
+                                             col_rel_residual.empty() ? nullptr : col_rel_residual.data(), stream);
+        if (rc != DIMGPU_OK && (throw_on_failure || (rc != DIMGPU_ERR_NOT_CONVERGED && rc != DIMGPU_ERR_BREAKDOWN)))
+            raise(rc);
+        return st;
+    }
+
+private:
+    void reset() noexcept {
+        if (h_)
+            dimgpu_block_cg_destroy(h_);
+        h_ = nullptr;
+    }
+    dimgpu_block_cg* h_{};
+    uint32_t k_{};
+};
+
+// The adjoint of x = A^{-1} b for a loss L(x): lambda := A^{-T} g (g = dL/dx, device memory; lambda holds
+// the initial guess on entry and dL/db on return) and, when grad_vals is given, dL/dA = -lambda x^T on
+// the pattern, in the CSR order of the matrix given to from_csr.
+inline dimgpu_cg_stats cg_adjoint(const csr5& a, const double* g, const double* x, double* lambda, double* grad_vals,
+                                  const dimgpu_cg_params& params, void* stream = nullptr) {
+    dimgpu_cg_stats st{};
+    check(dimgpu_cg_adjoint(a.handle(), g, x, lambda, grad_vals, &params, &st, stream));
+    return st;
+}
 
 // The reference's HDF5 matrix IO (dim::io::h5, include/dim/io/h5.h:68-115; libs/dim/io/h5.cpp:45-74).
 // File errors throw dim::gpu::error with DIMGPU_ERR_IO, a missing group std::invalid_argument.

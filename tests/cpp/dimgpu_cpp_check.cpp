@@ -1,6 +1,6 @@
 // A C++ caller of dimgpu through include/dimgpu.hpp, as a dim user would write it: from_csr, spmv on
 // host spans and on device memory (CUDA runtime allocations, a stream, the status query), the CG
-// solver, the reference's exceptions, and the file IO (HDF5: write_matlab_compatible and
+// solver, the SpMM, block CG and adjoint solve, the reference's exceptions, and the file IO (HDF5: write_matlab_compatible and
 // read_matlab_compatible, store and load_csr5, the result vector; Matrix Market: load_matrix_market).
 //
 //   dimgpu_cpp_check <output file>
@@ -119,6 +119,55 @@ int main(int argc, char** argv) {
     const dimgpu_cg_stats st = solver.solve(y, z);
     EXPECT(st.status == DIMGPU_OK && st.rel_residual <= 1.5e-10);
     A.status();
+
+    // the batched and differentiated forms: an SpMM with two copies of x, a block CG on [y, 2 y], and the
+    // adjoint solve of A lambda = y (A is symmetric); all on device memory
+    {
+        std::vector<double> X2(2 * n), Y2(2 * n), B2(2 * n), Z2(2 * n, 0.0);
+        for (uint32_t i = 0; i < n; ++i) {
+            X2[2 * i] = X2[2 * i + 1] = x[i];
+            B2[2 * i] = y[i];
+            B2[2 * i + 1] = 2.0 * y[i];
+        }
+        double *dX2 = nullptr, *dY2 = nullptr, *dB2 = nullptr, *dZ2 = nullptr, *dl = nullptr, *dg = nullptr;
+        EXPECT(cudaMalloc(&dX2, 2 * n * sizeof(double)) == cudaSuccess && cudaMalloc(&dY2, 2 * n * sizeof(double)) == cudaSuccess);
+        EXPECT(cudaMalloc(&dB2, 2 * n * sizeof(double)) == cudaSuccess && cudaMalloc(&dZ2, 2 * n * sizeof(double)) == cudaSuccess);
+        EXPECT(cudaMalloc(&dl, n * sizeof(double)) == cudaSuccess && cudaMalloc(&dg, n * sizeof(double)) == cudaSuccess);
+        EXPECT(cudaMemcpy(dX2, X2.data(), 2 * n * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess);
+        A.spmm_device(2, dX2, 2, dY2, 2);
+        EXPECT(cudaMemcpy(Y2.data(), dY2, 2 * n * sizeof(double), cudaMemcpyDeviceToHost) == cudaSuccess);
+        for (uint32_t i = 0; i < n; ++i)
+            EXPECT(std::fabs(Y2[2 * i] - y[i]) <= 1e-12 * 8.0 && Y2[2 * i + 1] == Y2[2 * i]);
+        EXPECT(cudaMemcpy(dB2, B2.data(), 2 * n * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess);
+        EXPECT(cudaMemcpy(dZ2, Z2.data(), 2 * n * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess);
+        dim::gpu::block_cg_solver bcg(A, 2, p);
+        std::vector<int64_t> its(2);
+        std::vector<double> rel(2);
+        const dimgpu_block_cg_stats bst = bcg.solve_device(dB2, 2, dZ2, 2, its, rel);
+        EXPECT(bst.converged_columns == 2 && rel[0] <= 1.5e-10 && rel[1] <= 1.5e-10);
+        EXPECT(cudaMemcpy(Z2.data(), dZ2, 2 * n * sizeof(double), cudaMemcpyDeviceToHost) == cudaSuccess);
+        for (uint32_t i = 0; i < n; ++i)  // A z = A x: the solutions are x and 2 x
+            EXPECT(std::fabs(Z2[2 * i] - x[i]) <= 1e-6 && std::fabs(Z2[2 * i + 1] - 2.0 * x[i]) <= 2e-6);
+        // adjoint: lambda = A^{-T} y = x (A symmetric, y = A x), dL/dA on the pattern = -lambda x^T
+        std::vector<double> zero(n, 0.0), grad(v.size());
+        double* dgrad = nullptr;
+        EXPECT(cudaMalloc(&dgrad, v.size() * sizeof(double)) == cudaSuccess);
+        EXPECT(cudaMemcpy(dg, y.data(), n * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess);
+        EXPECT(cudaMemcpy(dl, zero.data(), n * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess);
+        EXPECT(cudaMemcpy(dX2, x.data(), n * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess);
+        const dimgpu_cg_stats ast = dim::gpu::cg_adjoint(A, dg, dX2, dl, dgrad, p);
+        EXPECT(ast.status == DIMGPU_OK);
+        std::vector<double> lam(n);
+        EXPECT(cudaMemcpy(lam.data(), dl, n * sizeof(double), cudaMemcpyDeviceToHost) == cudaSuccess);
+        EXPECT(cudaMemcpy(grad.data(), dgrad, v.size() * sizeof(double), cudaMemcpyDeviceToHost) == cudaSuccess);
+        for (uint32_t i = 0; i < n; ++i) {
+            EXPECT(std::fabs(lam[i] - x[i]) <= 1e-6);
+            for (uint32_t e = rp[i]; e < rp[i + 1]; ++e)
+                EXPECT(grad[e] == -lam[i] * x[ci[e]]);
+        }
+        for (double* q : {dX2, dY2, dB2, dZ2, dl, dg, dgrad})
+            cudaFree(q);
+    }
 
     // HDF5 round trips next to the output file: the matrix through its MATLAB-compatible group and its
     // CSR5 group (converted with the reference's layout), the solution as a result vector
