@@ -52,8 +52,10 @@ def test_block_cg_masks(native, torch_cuda):
     np.testing.assert_allclose(Xd.cpu().numpy()[:, [0, 3]], xs[:, [0, 3]], atol=1e-7)
 
 
-@pytest.mark.parametrize("k", [8, 32])
+@pytest.mark.parametrize("k", [3, 8, 16, 32])
 def test_block_cg_mixed(native, torch_cuda, k):
+    """Mixed block CG at widths whose f32 SpMM holds four right-hand sides per lane with idle lanes
+    (k = 3: padded to 4) and without (8, 16, 32)."""
     torch = torch_cuda
     m = laplacian_3d_7pt(20)
     n = m.dimensions.rows
