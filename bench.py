@@ -400,6 +400,8 @@ def run_spmv_only(args):
         m = m.permuted(m.hub_first_order())
     n, nnz = m.dimensions.rows, m.nnz
     A = csr5.from_csr(m)
+    if args.gather_ceiling:
+        return _gather_ceiling(A, m)
     if args.all_launches:
         return _time_all_launches(A, n)
     stream = torch.cuda.current_stream()
@@ -448,6 +450,77 @@ def _time_all_launches(A, n):
                 ev1.record(stream)
                 torch.cuda.synchronize()
                 out[f"{'f32' if f32 else 'f64'}_{w}_{g}_us"] = ev0.elapsed_time(ev1) / 30 * 1e3
+    print(json.dumps(out))
+    return 0
+
+
+def _gather_ceiling(A, m):
+    """The SpMV against the gather-only kernels of libdimgpu_probe.so (CUDA events, 30 launches each):
+    x[col] summed over the matrix's own column indices in CSR order, f64 and f32 x, L1-allocating and
+    L1-bypassing loads -- the rate at which the random gathers alone can run -- and, over the same number
+    of uniform random indices, f32 gathers from all of x, from the distributed shared memory of
+    thread-block clusters of 2-16 CTAs and from each CTA's own shared memory."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from diploma_research_gb300 import build as B
+
+    P = ctypes.CDLL(B.build(variant="probe"))
+    P.dimgpu_probe_words_per_cta.restype = ctypes.c_uint32
+    P.dimgpu_probe_gather.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint32,
+                                      ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                      ctypes.POINTER(ctypes.c_float)]
+    P.dimgpu_probe_cluster_gather.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int, ctypes.c_int,
+                                              ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_float),
+                                              ctypes.POINTER(ctypes.c_int)]
+    n, nnz = m.dimensions.rows, m.nnz
+    stream = torch.cuda.current_stream()
+    reps = 30
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    x = torch.tensor(np.random.default_rng(5).uniform(-1, 1, n), device="cuda", dtype=torch.float64)
+    y = torch.empty(n, device="cuda", dtype=torch.float64)
+    x32, y32 = x.float(), torch.empty(n, device="cuda", dtype=torch.float32)
+    out = {"n": n, "nnz": nnz, "reps": reps, "launch_f64": A.spmv_launch(False), "launch_f32": A.spmv_launch(True)}
+    for name, xx, yy in (("spmv_f64_us", x, y), ("spmv_f32_us", x32, y32)):
+        for _ in range(5):
+            A.spmv(xx, yy)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(reps):
+            A.spmv(xx, yy)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = ev0.elapsed_time(ev1) / reps * 1e3
+    col = torch.from_numpy(m.col_indices.astype(np.int32)).to("cuda")
+    us, ctas = ctypes.c_float(), ctypes.c_int()
+    for tag, xx in (("f64", x), ("f32", x32)):
+        for bypass in (0, 1):
+            rc = P.dimgpu_probe_gather(col.data_ptr(), nnz, xx.data_ptr(), n, xx.element_size(), bypass, reps,
+                                       stream.cuda_stream, ctypes.byref(us))
+            if rc:
+                raise RuntimeError(f"dimgpu_probe_gather: CUDA error {rc}")
+            out[f"gather_{tag}_{'l1_bypass' if bypass else 'l1'}_us"] = us.value
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    q = torch.randint(0, n, (nnz,), device="cuda", dtype=torch.int32, generator=gen)
+    rc = P.dimgpu_probe_gather(q.data_ptr(), nnz, x32.data_ptr(), n, 4, 0, reps, stream.cuda_stream,
+                               ctypes.byref(us))
+    if rc:
+        raise RuntimeError(f"dimgpu_probe_gather: CUDA error {rc}")
+    out["gather_f32_uniform_random_us"] = us.value  # as many indices, uniform over all of x
+    del q
+    w = int(P.dimgpu_probe_words_per_cta())
+    out["cluster_words_per_cta"] = w
+    for cl in (2, 4, 8, 16):
+        for local in (0, 1):
+            span = w if local else cl * w
+            q = torch.randint(0, span, (nnz,), device="cuda", dtype=torch.int32, generator=gen)
+            rc = P.dimgpu_probe_cluster_gather(q.data_ptr(), nnz, cl, local, reps, stream.cuda_stream,
+                                               ctypes.byref(us), ctypes.byref(ctas))
+            key = f"cluster{cl}_{'own_smem' if local else 'dsmem'}"
+            out[key] = {"us": us.value, "ctas": ctas.value, "span_words": span} if rc == 0 else {"cuda_error": rc}
+            del q
     print(json.dumps(out))
     return 0
 
@@ -665,6 +738,8 @@ def main():
                     help="with --spmv-only: the matrix as generated or renumbered by decreasing row length")
     ap.add_argument("--all-launches", action="store_true",
                     help="with --spmv-only: time the f64 and f32 SpMV in every launch configuration")
+    ap.add_argument("--gather-ceiling", action="store_true",
+                    help="with --spmv-only: the SpMV against gather-only kernels over its column indices")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven CG loop instead of the CUDA graph (profilers list every kernel)")
     ap.add_argument("--batch", default=None, help="comma-separated k: the multi-RHS block-CG workload")

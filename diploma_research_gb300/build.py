@@ -7,6 +7,9 @@ CUDA runtime statically and depends on nothing from PyTorch.
 DIMGPU_TEST_HOOKS defined and a 20 ms limit on every bounded device wait (DIMGPU_WAIT_NS): it adds
 hooks that make a wait run out on purpose, for the tests of the device status words.  The product
 never loads it.
+
+``build(variant="probe")`` builds libdimgpu_probe.so from probe/*.cu: gather-only kernels that bench.py
+times to measure the random-gather ceiling of an SpMV (``bench.py --spmv-only --gather-ceiling``).
 """
 from __future__ import annotations
 
@@ -23,6 +26,8 @@ OUT_DIR = os.path.join(HERE, "_lib")
 BUILD_DIR = os.path.join(ROOT, "_build", "dimgpu")
 LIB = os.path.join(OUT_DIR, "libdimgpu.so")
 TEST_LIB = os.path.join(OUT_DIR, "libdimgpu_test.so")
+PROBE_LIB = os.path.join(OUT_DIR, "libdimgpu_probe.so")
+PROBE_SRC = os.path.join(HERE, "probe")
 TEST_FLAGS = ["-DDIMGPU_TEST_HOOKS", "-DDIMGPU_WAIT_NS=20000000ull"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -37,8 +42,9 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libdimgpu")
 
 
-def sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
+def sources(variant: str = "product"):
+    d = PROBE_SRC if variant == "probe" else CSRC
+    return sorted(os.path.join(d, f) for f in os.listdir(d) if f.endswith((".cu", ".cpp")))
 
 
 def headers():
@@ -64,7 +70,8 @@ def _run(cmd, verbose):
 
 
 def build(verbose: bool = False, force: bool = False, extra_flags=(), variant: str = "product") -> str:
-    """Builds one variant ("product": libdimgpu.so, "test": libdimgpu_test.so); returns its path."""
+    """Builds one variant ("product": libdimgpu.so, "test": libdimgpu_test.so, "probe":
+    libdimgpu_probe.so); returns its path."""
     return build_variants((variant,), verbose=verbose, force=force, extra_flags=extra_flags)[0]
 
 
@@ -75,15 +82,15 @@ def build_variants(variants=("product", "test"), verbose: bool = False, force: b
     os.makedirs(OUT_DIR, exist_ok=True)
     jobs, links = [], []
     for variant in variants:
-        if variant not in ("product", "test"):
+        if variant not in ("product", "test", "probe"):
             raise ValueError(f"unknown variant {variant!r}")
-        lib_path = TEST_LIB if variant == "test" else LIB
-        build_dir = BUILD_DIR + ("_test" if variant == "test" else "")
+        lib_path = {"product": LIB, "test": TEST_LIB, "probe": PROBE_LIB}[variant]
+        build_dir = BUILD_DIR + ("" if variant == "product" else "_" + variant)
         flags = list(extra_flags) + (TEST_FLAGS if variant == "test" else [])
         os.makedirs(build_dir, exist_ok=True)
         objs, fresh = [], False
-        for src in sources():
-            obj = os.path.join(build_dir, os.path.basename(src)[:-3] + ".o")
+        for src in sources(variant):
+            obj = os.path.join(build_dir, os.path.splitext(os.path.basename(src))[0] + ".o")
             objs.append(obj)
             if force or _stale(obj, [src] + hdrs):
                 jobs.append([nv, *ARCH, *NVCC_FLAGS, *flags, "-c", src, "-o", obj])
