@@ -48,10 +48,22 @@ struct vec_ctx {
     int has_loop, has_ru;
 };
 
+// Sums the kWarps values v[0..kWarps) in warp 0 by a shuffle tree (a fixed order); lane 0 gets the total.
+constexpr int kWarps = kVecThreads / 32;
+static_assert(kWarps <= 32 && (kWarps & (kWarps - 1)) == 0, "the shuffle tree takes a power of two");
+__device__ __forceinline__ double warp0_tree(const double* v, unsigned lane) {
+    double x = lane < (unsigned)kWarps ? v[lane] : 0.0;
+#pragma unroll
+    for (int d = kWarps / 2; d > 0; d >>= 1)
+        x += __shfl_xor_sync(kFull, x, d);
+    return x;
+}
+
 // Reduces (a, b) over the grid.  Returns true in exactly one thread (thread 0 of the last block to
-// finish) with the totals in *ta, *tb, summed in block order.
+// finish) with the totals in *ta, *tb, summed in a fixed order (warps by shuffles, the warps of a block
+// and the blocks' partials by shuffle trees), so the result does not depend on which block is last.
 __device__ bool grid_reduce2(double a, double b, const vec_ctx& c, double* ta, double* tb) {
-    __shared__ double sa[kVecThreads / 32], sb[kVecThreads / 32];
+    __shared__ double sa[kWarps], sb[kWarps];
     __shared__ uint32_t s_last;
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     a = warp_sum(a);
@@ -61,15 +73,13 @@ __device__ bool grid_reduce2(double a, double b, const vec_ctx& c, double* ta, d
         sb[warp] = b;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double x = 0, y = 0;
-        for (int w = 0; w < kVecThreads / 32; ++w) {
-            x += sa[w];
-            y += sb[w];
+    if (warp == 0) {
+        const double x = warp0_tree(sa, lane), y = warp0_tree(sb, lane);
+        if (lane == 0) {
+            c.part[2 * blockIdx.x] = x;
+            c.part[2 * blockIdx.x + 1] = y;
+            s_last = (ticket_acq_rel(c.counter) == gridDim.x - 1) ? 1u : 0u;
         }
-        c.part[2 * blockIdx.x] = x;
-        c.part[2 * blockIdx.x + 1] = y;
-        s_last = (ticket_acq_rel(c.counter) == gridDim.x - 1) ? 1u : 0u;
     }
     __syncthreads();
     if (!s_last)
@@ -87,14 +97,12 @@ __device__ bool grid_reduce2(double a, double b, const vec_ctx& c, double* ta, d
         sb[warp] = y;
     }
     __syncthreads();
-    if (threadIdx.x != 0)
+    if (warp != 0)
         return false;
-    x = 0;
-    y = 0;
-    for (int w = 0; w < kVecThreads / 32; ++w) {
-        x += sa[w];
-        y += sb[w];
-    }
+    x = warp0_tree(sa, lane);
+    y = warp0_tree(sb, lane);
+    if (lane != 0)
+        return false;
     *ta = x;
     *tb = y;
     *c.counter = 0u;
@@ -140,8 +148,13 @@ __device__ __forceinline__ void vloop(uint64_t nv, Ld load, Op op) {
 // vector kernel's 2 DFMA per element the pipe is busy for about as long as the loads take).  load(i, slot)
 // and op(i, slot) use slots [0, U) and [U, 2U) in turn; indices at or past nv are skipped, so a last
 // partial round costs one memory round trip, not one per index.
-template <int U, typename Ld, typename Op>
-__device__ __forceinline__ void vloop_pipe(uint64_t nv, Ld load, Op op) {
+//
+// gate() is evaluated after the first round's loads are issued and before any op; when it returns false
+// the loop does nothing more and vloop_pipe returns false.  A kernel whose work depends on solver state
+// written by the previous kernel reads that state inside gate(), so the state's load latency overlaps
+// the first round's loads (only loads of the vector data happen before the gate: nothing is written).
+template <int U, typename Ld, typename Op, typename Gate>
+__device__ __forceinline__ bool vloop_pipe(uint64_t nv, Ld load, Op op, Gate gate) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t span = U * stride;
     uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
@@ -158,6 +171,8 @@ __device__ __forceinline__ void vloop_pipe(uint64_t nv, Ld load, Op op) {
                 op(i0 + u * stride, base + u);
     };
     ld_round(i, 0);
+    if (!gate())
+        return false;
     while (i < nv) {
         ld_round(i + span, U);
         op_round(i, 0);
@@ -168,6 +183,12 @@ __device__ __forceinline__ void vloop_pipe(uint64_t nv, Ld load, Op op) {
         op_round(i, U);
         i += span;
     }
+    return true;
+}
+
+template <int U, typename Ld, typename Op>
+__device__ __forceinline__ void vloop_pipe(uint64_t nv, Ld load, Op op) {
+    vloop_pipe<U>(nv, load, op, [] { return true; });
 }
 
 // The scalar elements past the last full vector, visited by the first threads of block 0.
@@ -227,21 +248,15 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_init64(const double* b, cons
 // r -= alpha As; rr' = r.r; decide
 __global__ void __launch_bounds__(kVecThreads, 2) k_update_r64(const double* As, double* r, uint64_t n, vec_ctx c) {
     cg_state* st = c.st;
-    // the state was written by earlier kernels: read it once, both words in flight together
+    // the state was written by earlier kernels: read it once, both words in flight together and with
+    // the first round's vector loads
     const uint32_t stop = st->stop;
     const double alpha = st->alpha;
-    if (stop) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            st->x_pending = 0;
-            set_loop(c, false);
-        }
-        return;
-    }
     const uint64_t pol = policy_evict_last();
-    double rr = 0;
+    double rrx = 0, rry = 0;  // two independent chains of the r.r accumulation
     constexpr int U = 2;
     double2 av[2 * U], qv[2 * U];
-    vloop_pipe<U>(
+    const bool go = vloop_pipe<U>(
         n / 2,
         [&](uint64_t i, int u) {
             av[u] = ld2_keep(As + 2 * i, pol);
@@ -253,15 +268,24 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_update_r64(const double* As,
             q.x = fma(-alpha, a.x, q.x);
             q.y = fma(-alpha, a.y, q.y);
             st2_stream(r + 2 * i, q, pol);
-            rr = fma(q.x, q.x, fma(q.y, q.y, rr));
-        });
+            rrx = fma(q.x, q.x, rrx);
+            rry = fma(q.y, q.y, rry);
+        },
+        [&] { return stop == 0u; });
+    if (!go) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            st->x_pending = 0;
+            set_loop(c, false);
+        }
+        return;
+    }
     vtail(n, 2, [&](uint64_t i) {
         const double ri = fma(-alpha, As[i], r[i]);
         r[i] = ri;
-        rr = fma(ri, ri, rr);
+        rrx = fma(ri, ri, rrx);
     });
     double t, unused;
-    if (grid_reduce2(rr, 0.0, c, &t, &unused)) {
+    if (grid_reduce2(rrx + rry, 0.0, c, &t, &unused)) {
         st->rr_new = t;
         st->iter += 1;
         st->x_pending = 1;
@@ -281,27 +305,28 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_update_r64(const double* As,
 // x += alpha s; s = r + beta s (the latter only while the solve continues)
 __global__ void __launch_bounds__(kVecThreads, 2) k_update_xs64(double* x, double* s, const double* r, uint64_t n,
                                                              const cg_state* st) {
+    // the state read overlaps the first round's loads of the continuing solve's update (the usual case)
     const uint32_t pending = st->x_pending, stop = st->stop;
     const double alpha = st->alpha, beta = st->beta;
-    if (!pending)
-        return;
     const uint64_t pol = policy_evict_last();
-    const bool more = !stop;
     constexpr int U = 1;  // three 16-byte loads per element, two rounds in flight: 24 registers of data
     double2 sv[2 * U], xv[2 * U], rv[2 * U];
+    const bool more = vloop_pipe<U>(
+        n / 2,
+        [&](uint64_t i, int u) {
+            sv[u] = ld2_keep(s + 2 * i, pol);
+            xv[u] = ld2_keep(x + 2 * i, pol);
+            rv[u] = ld2_keep(r + 2 * i, pol);
+        },
+        [&](uint64_t i, int u) {
+            const double2 si = sv[u], xi = xv[u], ri = rv[u];
+            st2_stream(x + 2 * i, make_double2(fma(alpha, si.x, xi.x), fma(alpha, si.y, xi.y)), pol);
+            st2_stream(s + 2 * i, make_double2(fma(beta, si.x, ri.x), fma(beta, si.y, ri.y)), pol);
+        },
+        [&] { return pending != 0u && stop == 0u; });
+    if (!pending)
+        return;
     if (more) {
-        vloop_pipe<U>(
-            n / 2,
-            [&](uint64_t i, int u) {
-                sv[u] = ld2_keep(s + 2 * i, pol);
-                xv[u] = ld2_keep(x + 2 * i, pol);
-                rv[u] = ld2_keep(r + 2 * i, pol);
-            },
-            [&](uint64_t i, int u) {
-                const double2 si = sv[u], xi = xv[u], ri = rv[u];
-                st2_stream(x + 2 * i, make_double2(fma(alpha, si.x, xi.x), fma(alpha, si.y, xi.y)), pol);
-                st2_stream(s + 2 * i, make_double2(fma(beta, si.x, ri.x), fma(beta, si.y, ri.y)), pol);
-            });
         vtail(n, 2, [&](uint64_t i) {
             const double si = s[i];
             x[i] = fma(alpha, si, x[i]);
@@ -384,21 +409,14 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_init_mixed(const double* b, 
 __global__ void __launch_bounds__(kVecThreads, 2) k_update_r_mixed(const float* As, float* r, const float* s, float* y,
                                                                 uint64_t n, vec_ctx c) {
     cg_state* st = c.st;
+    // the state read overlaps the first round's loads
     const uint32_t stop = st->stop;
     const float af = (float)st->alpha;
-    if (stop) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            st->no_ru = 1;
-            set_ru(c, false);
-            set_loop(c, false);
-        }
-        return;
-    }
     const uint64_t pol = policy_evict_last();
     double rr = 0;
     constexpr int U = 1;  // four 16-byte loads per element, two rounds in flight
     float4 av[2 * U], sv[2 * U], qv[2 * U], yv[2 * U];
-    vloop_pipe<U>(
+    const bool go = vloop_pipe<U>(
         n / 4,
         [&](uint64_t i, int u) {
             av[u] = ld4_keep(As + 4 * i, pol);
@@ -415,7 +433,16 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_update_r_mixed(const float* 
             st4_stream(r + 4 * i, q, pol);
             st4_stream(y + 4 * i, yi, pol);
             rr += (double)sq4(q);
-        });
+        },
+        [&] { return stop == 0u; });
+    if (!go) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            st->no_ru = 1;
+            set_ru(c, false);
+            set_loop(c, false);
+        }
+        return;
+    }
     vtail(n, 4, [&](uint64_t i) {
         const float q = fmaf(-af, As[i], r[i]);
         r[i] = q;
