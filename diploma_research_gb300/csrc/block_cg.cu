@@ -63,7 +63,8 @@ __device__ __forceinline__ void bset(cudaGraphConditionalHandle h, int has, bool
 }
 
 // Per-column grid reduction of two values (thread's column = threadIdx.x % kp).  Returns true in every
-// thread of the last block; then t1[j], t2[j] (j < kp) hold column j's totals, summed in block order.
+// thread of the last block; then t1[j], t2[j] (j < kp) hold column j's totals, summed in a fixed order
+// (the blocks' partials in kThreads / 32 interleaved slices, then the slices in order).
 __device__ bool grid_reduce_cols(double v1, double v2, uint32_t kp, const bctx& c, double* t1, double* t2) {
     __shared__ double s_w[kThreads / 32][64];
     __shared__ uint32_t s_last;
@@ -92,11 +93,24 @@ __device__ bool grid_reduce_cols(double v1, double v2, uint32_t kp, const bctx& 
     __syncthreads();
     if (!s_last)
         return false;
+    // the blocks' partials: warp w sums blocks w, w + W, w + 2W, ... of its lane's column, then one thread
+    // per column sums the W slices in warp order (a fixed order whichever block is last)
+    constexpr unsigned W = kThreads / 32;
+    if (lane < kp) {
+        double a = 0, b = 0;
+        for (unsigned blk = warp; blk < gridDim.x; blk += W) {
+            a += __ldcg(&c.part[(uint64_t)blk * 64 + lane]);
+            b += __ldcg(&c.part[(uint64_t)blk * 64 + 32 + lane]);
+        }
+        s_w[warp][lane] = a;
+        s_w[warp][32 + lane] = b;
+    }
+    __syncthreads();
     if (threadIdx.x < kp) {
         double a = 0, b = 0;
-        for (unsigned blk = 0; blk < gridDim.x; ++blk) {
-            a += __ldcg(&c.part[(uint64_t)blk * 64 + threadIdx.x]);
-            b += __ldcg(&c.part[(uint64_t)blk * 64 + 32 + threadIdx.x]);
+        for (unsigned w = 0; w < W; ++w) {
+            a += s_w[w][threadIdx.x];
+            b += s_w[w][32 + threadIdx.x];
         }
         t1[threadIdx.x] = a;
         t2[threadIdx.x] = b;

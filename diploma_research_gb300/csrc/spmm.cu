@@ -762,13 +762,16 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmm(const spmm_params<VT> p) {
         }
     }
     if constexpr (DOT) {
+        // the CTAs' partials in WPC interleaved slices (warp w: CTAs w, w + WPC, ...) beside the warp's
+        // tail rows, then the slices in warp order: a fixed order whichever CTA is last
+        double dw = fix_dot;
+        for (uint32_t c = warp; c < gridDim.x; c += WPC)
+            dw += __ldcg(&p.cta_part[(uint64_t)c * 32 + lane]);
         __syncthreads();
-        s_dot[warp][lane] = fix_dot;
+        s_dot[warp][lane] = dw;
         __syncthreads();
         if (warp == 0) {
             double d = 0.0;
-            for (uint32_t c = 0; c < gridDim.x; ++c)
-                d += __ldcg(&p.cta_part[(uint64_t)c * 32 + lane]);
             for (int w = 0; w < WPC; ++w)
                 d += s_dot[w][lane];
             if (lane_on) {

@@ -116,6 +116,18 @@ __device__ VT close_row(const spmv_params<VT>& p, uint32_t run, uint32_t R, VT o
     return acc + own;
 }
 
+// The sum of v[0..N) for N <= 32 in warp 0: a shuffle tree over 32 lanes (lanes >= N add 0), in a fixed
+// order; every lane gets the total.
+template <int N>
+__device__ __forceinline__ double warps_total(const double* v, unsigned lane) {
+    static_assert(N >= 1 && N <= 32, "one value per lane");
+    double x = lane < (unsigned)N ? v[lane] : 0.0;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1)
+        x += __shfl_xor_sync(kFull, x, d);
+    return x;
+}
+
 template <typename VT, int SIGMA, int WPC, int STAGES, bool DOT, int XM, bool IDX16>
 __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
     using G = tile_geom<VT, SIGMA, IDX16>;
@@ -262,15 +274,16 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
 
     // ---- completion ticket; the last CTA computes the CSR tail and the epilogue ----
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (warp == 0) {
         if constexpr (DOT) {
-            double d = 0.0;
-            for (int w = 0; w < WPC; ++w)
-                d += s_red[w];
-            p.cta_part[cta] = d;
+            const double d = warps_total<WPC>(s_red, lane);  // the CTA's warp partials, a fixed shuffle tree
+            if (lane == 0)
+                p.cta_part[cta] = d;
         }
-        const uint32_t ticket = ticket_acq_rel(&p.words[0]);
-        s_last = (ticket == gridDim.x - 1) ? 1u : 0u;
+        if (lane == 0) {
+            const uint32_t ticket = ticket_acq_rel(&p.words[0]);
+            s_last = (ticket == gridDim.x - 1) ? 1u : 0u;
+        }
     }
     __syncthreads();
     if (!s_last)
@@ -303,10 +316,8 @@ __global__ void __launch_bounds__(WPC * 32, 1) k_spmv(const spmv_params<VT> p) {
         if (lane == 0)
             s_red[warp] = part;
         __syncthreads();
+        const double dot = warp == 0 ? warps_total<WPC>(s_red, lane) : 0.0;
         if (threadIdx.x == 0) {
-            double dot = 0.0;
-            for (int wi = 0; wi < WPC; ++wi)
-                dot += s_red[wi];
             if (p.dot_out)
                 *p.dot_out = dot;
             if (p.rr) {
