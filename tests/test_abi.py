@@ -68,3 +68,17 @@ def test_product_does_not_import_oracle():
                 src = open(os.path.join(dirpath, f)).read()
                 assert not re.search(r"^\s*(import|from)\s+oracle", src, re.M), f
                 assert "csr5_oracle" not in src, f
+
+
+def test_probe_library_builds_apart_from_the_product(native):
+    """libdimgpu_probe.so (the gather-only kernels bench.py --spmv-only --gather-ceiling times) builds from
+    probe/*.cu alone and exports only its measurement entry points; the product library contains none."""
+    from diploma_research_gb300 import build as B
+
+    path = B.build(variant="probe")
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    assert {s for s in exported if s.startswith("dimgpu_")} == {
+        "dimgpu_probe_words_per_cta", "dimgpu_probe_gather", "dimgpu_probe_cluster_gather"}
+    prod = subprocess.run(["nm", "-D", "--defined-only", N.LIB_PATH], capture_output=True, text=True).stdout
+    assert "dimgpu_probe_" not in prod
