@@ -57,3 +57,39 @@ def test_reference_arm_only_on_rank_zero(monkeypatch, capsys):
 
     assert bench.run_reference(A()) == 0
     assert capsys.readouterr().out == ""  # rank 1 prints nothing and does no work
+
+
+def test_reference_arm_line_on_rank_zero(monkeypatch, capsys):
+    """Rank 0 prints the reference arm's one JSON line with the keys of the benchmark contract: full CPU CG
+    solves by the oracle (one per step, no extrapolation), a cpu_baseline describing the run, an e2e equal
+    to the value with no host-device bytes, and the same config string as the GPU arm for the system."""
+    import json
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        monkeypatch.delenv(k, raising=False)
+    monkeypatch.setattr(bench, "WORKLOAD", "lap2d_512")
+    monkeypatch.setattr(bench, "TOL", 1e-8)
+
+    class A:
+        gpus, steps, warmup = 1, 1, 0
+
+    assert bench.run_reference(A()) == 0
+    lines = [ln for ln in capsys.readouterr().out.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in d, key
+    assert d["impl"] == "reference" and d["unit"] == "s" and d["higher_is_better"] is False
+    assert d["value"] > 0 and abs(d["ms_per_step"] - 1e3 * d["value"]) < 1e-9
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
+    assert d["cpu_baseline"]["cores"] >= 1 and "lap2d_512" in d["cpu_baseline"]["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    # 939 iterations to 1e-8 on the 512^2 Laplacian, as the reference's dim_sp loop takes
+    assert d["iterations"] == 939
+    from diploma_research_gb300.generators import WORKLOADS
+
+    assert d["config"] == bench._config(WORKLOADS["lap2d_512"]["build"]())
