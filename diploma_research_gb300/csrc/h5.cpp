@@ -434,7 +434,7 @@ public:
     // `limit`: the most bytes the stream may produce (a chunk's size); a stream that would produce more is
     // not a chunk of this dataset
     inflater(const uint8_t* in, size_t n, std::vector<uint8_t>& out, size_t limit)
-        : in_(in), n_(n), out_(out), limit_(limit) {}
+        : in_(in), n_(n), out_(out), limit_(limit), start_(out.size()) {}
 
     void run() {
         if (n_ < 2)
@@ -456,9 +456,38 @@ public:
             else
                 throw format_error("deflate chunk: invalid block type");
         }
+        // the zlib trailer: Adler-32 (RFC 1950 section 8) of the bytes this stream produced, big-endian,
+        // at the next byte boundary; a mismatch is a corrupt chunk, as libhdf5's deflate filter reports it
+        buf_ = 0;
+        cnt_ = 0;
+        if (pos_ + 4 > n_)
+            throw format_error("deflate chunk: truncated (no Adler-32 check value)");
+        const uint32_t want = ((uint32_t)in_[pos_] << 24) | ((uint32_t)in_[pos_ + 1] << 16) |
+                              ((uint32_t)in_[pos_ + 2] << 8) | (uint32_t)in_[pos_ + 3];
+        if (adler32(out_.data() + start_, out_.size() - start_) != want)
+            throw format_error("deflate chunk: Adler-32 check value does not match");
     }
 
 private:
+    // Adler-32 (RFC 1950): a = 1 + the sum of the bytes, b = the sum of the successive a, both mod 65521.
+    // The sums are reduced every 5552 bytes, the most after which b still fits in 32 bits.
+    static uint32_t adler32(const uint8_t* p, size_t n) {
+        constexpr uint32_t kMod = 65521;
+        uint32_t a = 1, b = 0;
+        while (n) {
+            const size_t k = n < 5552 ? n : 5552;
+            for (size_t i = 0; i < k; ++i) {
+                a += p[i];
+                b += a;
+            }
+            a %= kMod;
+            b %= kMod;
+            p += k;
+            n -= k;
+        }
+        return (b << 16) | a;
+    }
+
     struct huffman {
         uint16_t count[16] = {};  // codes of each length
         uint16_t symbol[320] = {};  // symbols ordered by code
@@ -632,6 +661,7 @@ private:
     int cnt_ = 0;
     std::vector<uint8_t>& out_;
     size_t limit_;
+    size_t start_;  // out_'s size before this stream
 };
 
 // ------------------------------------------------------------------------------------------------
@@ -688,6 +718,21 @@ struct msg {
     uint16_t size;
 };
 
+// a * b, or a format error when the product of sizes read from the file does not fit in 64 bits
+uint64_t checked_mul(uint64_t a, uint64_t b, const char* what) {
+    uint64_t r = 0;
+    if (__builtin_mul_overflow(a, b, &r))
+        throw format_error(std::string(what) + ": size overflows 64 bits");
+    return r;
+}
+
+// the host's physical memory in bytes: no dataset larger than it is read (a corrupt dataspace must not
+// size an allocation the system cannot back)
+uint64_t host_memory_bytes() {
+    const long pages = sysconf(_SC_PHYS_PAGES), page = sysconf(_SC_PAGE_SIZE);
+    return (pages > 0 && page > 0) ? (uint64_t)pages * (uint64_t)page : std::numeric_limits<uint64_t>::max();
+}
+
 struct dataset_info {
     etype t;
     std::vector<uint64_t> shape;
@@ -697,9 +742,10 @@ struct dataset_info {
     uint64_t count() const {
         uint64_t n = 1;
         for (uint64_t d : shape)
-            n *= d;
+            n = checked_mul(n, d, "dataspace");
         return n;
     }
+    uint64_t bytes() const { return checked_mul(count(), t.element_bytes(), "dataset"); }
 };
 
 // datatype at p (inside a message of `n` bytes from `start`); returns the type and advances p
@@ -731,9 +777,11 @@ etype parse_type(const uint8_t* start, size_t n, size_t& p) {
         for (int d = 0; d < nd; ++d) {
             if (q + 4 > n)
                 throw format_error("truncated array datatype");
-            inner *= rd32(start + q);
+            inner = checked_mul(inner, rd32(start + q), "array datatype");
             q += 4;
         }
+        if (inner == 0 || inner > 65536)
+            throw format_error("array datatype of " + std::to_string(inner) + " elements is not supported");
         if (ver < 3)
             q += 4 * nd;  // permutation indices
         etype b = parse_type(start, n, q);
@@ -900,9 +948,9 @@ public:
             p += rnd(ssz);
             uint64_t cnt = 1;
             for (uint64_t s : shape)
-                cnt *= s;
-            const uint64_t nb = cnt * t.element_bytes();
-            if (p + nb > m.size)
+                cnt = checked_mul(cnt, s, "attribute dataspace");
+            const uint64_t nb = checked_mul(cnt, t.element_bytes(), "attribute");
+            if (nb > m.size || p + nb > m.size)
                 throw format_error("truncated attribute value");
             out.push_back({name, t, std::vector<uint8_t>(d + p, d + p + nb), t.inner ? 0 : cnt});
         }
@@ -937,13 +985,29 @@ public:
     // element count of a dataset's first dimension (1 for a scalar)
     uint64_t length(uint64_t addr) const {
         const dataset_info di = info(addr);
+        check_extent(di);
         return di.shape.empty() ? 1 : di.shape[0];
+    }
+
+    // The dataset's bytes, checked against what the file can hold before anything is allocated: no more
+    // than the host's memory, and a contiguous dataset's stored size at least its dataspace's.
+    uint64_t check_extent(const dataset_info& di) const {
+        const uint64_t nbytes = di.bytes();
+        if (nbytes > host_memory_bytes())
+            throw format_error("dataset of " + std::to_string(nbytes) + " bytes exceeds the host's memory");
+        if (di.layout[1] == 1) {
+            if (di.layout_size < 18)
+                throw format_error("truncated layout message");
+            if (rd64(di.layout + 2) != kUndef && rd64(di.layout + 10) < nbytes)
+                throw format_error("contiguous dataset stores fewer bytes than its dataspace holds");
+        }
+        return nbytes;
     }
 
     // all the bytes of a dataset (zeros where nothing was written)
     std::vector<uint8_t> read(uint64_t addr, dataset_info* out_info = nullptr) const {
         dataset_info di = info(addr);
-        const uint64_t nbytes = di.count() * di.t.element_bytes();
+        const uint64_t nbytes = check_extent(di);
         std::vector<uint8_t> raw;
         const uint8_t* L = di.layout;
         const int cls = L[1];
@@ -1081,8 +1145,10 @@ private:
             const uint8_t* raw = f_.at(child + base_, csize);
             const uint64_t n = std::min(chunk_elems, count - off0) * esz;
             if (deflate && !(fmask & 1)) {
+                // room for the bytes this chunk contributes (the layout's chunk size is only the limit the
+                // stream may not pass: a corrupt one must not size an allocation)
                 std::vector<uint8_t> plain;
-                plain.reserve(chunk_elems * esz);
+                plain.reserve(n);
                 inflater(raw, csize, plain, chunk_elems * esz).run();
                 if (plain.size() < n)
                     throw format_error("deflate chunk shorter than its elements");
@@ -1139,11 +1205,16 @@ node open_tree(const std::string& path, bool append) {
 // Elements of a dataset converted to T (as numpy's astype would; integers out of T's range are an error).
 template <typename T>
 std::vector<T> read_as(const reader& r, const std::string& path, uint64_t expect = kUndef) {
+    const uint64_t addr = r.resolve(path);
+    {  // the element count is checked before the dataset's bytes are read
+        const dataset_info d0 = r.info(addr);
+        const uint64_t n0 = checked_mul(d0.count(), d0.t.inner ? d0.t.inner : 1, "dataset");
+        if (expect != kUndef && n0 != expect)
+            throw format_error(path + ": " + std::to_string(n0) + " elements, expected " + std::to_string(expect));
+    }
     dataset_info di;
-    const std::vector<uint8_t> raw = r.read(r.resolve(path), &di);
+    const std::vector<uint8_t> raw = r.read(addr, &di);
     const uint64_t n = di.count() * (di.t.inner ? di.t.inner : 1);
-    if (expect != kUndef && n != expect)
-        throw format_error(path + ": " + std::to_string(n) + " elements, expected " + std::to_string(expect));
     std::vector<T> out(n);
     const uint8_t* p = raw.data();
     for (uint64_t i = 0; i < n; ++i, p += di.t.base) {
@@ -1386,8 +1457,9 @@ int dimgpu_h5_vector_length(const char* path, const char* dataset, uint64_t* n) 
         return fail(DIMGPU_ERR_INVALID_ARGUMENT, "NULL argument");
     return guarded("read_vector", [&] {
         reader r(path);
-        dataset_info di = r.info(r.resolve(dataset));
-        *n = di.count() * (di.t.inner ? di.t.inner : 1);
+        const dataset_info di = r.info(r.resolve(dataset));
+        r.check_extent(di);
+        *n = checked_mul(di.count(), di.t.inner ? di.t.inner : 1, "dataset");
         return DIMGPU_OK;
     });
 }

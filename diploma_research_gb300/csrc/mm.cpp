@@ -73,6 +73,7 @@ public:
     mapped& operator=(const mapped&) = delete;
     const char* begin() const { return p_; }
     const char* end() const { return p_ + n_; }
+    size_t size() const { return n_; }
 
 private:
     const char* p_ = nullptr;
@@ -179,6 +180,13 @@ csr_host load_as_csr(const char* path) {
     const uint64_t rows = parse_index(ss.token()), cols = parse_index(ss.token()), nnz = parse_index(ss.token());
     if (rows > 0xFFFFFFFFull || cols > 0xFFFFFFFFull)
         throw std::invalid_argument("matrix dimensions must fit in 32 bits");
+    // the size line sizes the allocations below: an entry takes at least four bytes ("1 1\n"), and the row
+    // arrays must fit in the host's memory
+    if (nnz > f.size() / 4)
+        throw std::invalid_argument("the size line claims more entries than the file holds");
+    const long pages = sysconf(_SC_PHYS_PAGES), page = sysconf(_SC_PAGE_SIZE);
+    if (pages > 0 && page > 0 && (rows + 1) * 12 > (uint64_t)pages * (uint64_t)page)
+        throw std::invalid_argument("the row count does not fit in the host's memory");
     // entries, in file order
     std::vector<uint32_t> r(nnz), c(nnz);
     std::vector<double> v(nnz, 1.0);

@@ -303,3 +303,120 @@ def test_reader_refuses_a_chunk_that_inflates_past_its_size(native, tmp_path, mo
     out = np.zeros(300)
     assert native.dimgpu_h5_read_vector(_b(p), b"Y", out.ctypes.data) == N.ERR_IO
     assert b"expands past" in native.dimgpu_last_error_string()
+
+
+def test_corrupt_compressed_chunk_is_refused(native, tmp_path, monkeypatch):
+    """A byte changed inside a deflate chunk whose stream still decodes (a stored block) is caught by the
+    zlib stream's Adler-32 check value, as libhdf5's deflate filter catches it, not returned as data."""
+    y = np.random.default_rng(2).uniform(-1, 1, 400)
+    p = tmp_path / "stored.h5"
+    monkeypatch.setattr(h5, "_write_dataset", _chunked_writer(chunk=100, compress=_deflate(0)))
+    h5.write_vector(p, "Y", y)
+    monkeypatch.undo()
+    assert np.array_equal(_c_read_vector(native, p, "Y"), y)
+    raw = bytearray(p.read_bytes())
+    at = bytes(raw).find(y[150:152].tobytes())  # chunk 1's stored bytes
+    assert at > 0
+    raw[at + 3] ^= 0x10
+    bad = tmp_path / "bad.h5"
+    bad.write_bytes(bytes(raw))
+    out = np.zeros(y.size)
+    assert native.dimgpu_h5_read_vector(_b(bad), b"Y", out.ctypes.data) == N.ERR_IO
+    assert b"Adler-32" in native.dimgpu_last_error_string()
+
+
+def _patch_u64(raw: bytearray, old: int, new: int, after: int) -> int:
+    """Replaces the first little-endian u64 `old` at or after `after`; returns its offset."""
+    at = bytes(raw).find(struct.pack("<Q", old), after)
+    assert at >= 0
+    raw[at:at + 8] = struct.pack("<Q", new)
+    return at
+
+
+def test_oversized_dataspaces_are_refused_before_allocating(native, tmp_path):
+    """A dataspace that claims more elements than the group's other datasets, than its stored bytes, or
+    than the host's memory is an error found before the dataset's bytes are allocated."""
+    m = random_csr(np.random.default_rng(8), 60, 50, 4.0)
+    p = tmp_path / "m.h5"
+    h5.write_matlab_compatible(p, "A", m)
+    h5.write_vector(p, "Y", np.arange(77.0))
+    raw = p.read_bytes()
+    rows, cols, nnz = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint64()
+    rp, ci, v = np.zeros(61, np.uint32), np.zeros(m.nnz, np.uint32), np.zeros(m.nnz)
+
+    # ir (the second dataset of nnz elements) claims 2^39 + nnz elements: refused against data's count
+    b = bytearray(raw)
+    first = _patch_u64(b, m.nnz, m.nnz, 0)  # data's dataspace stays
+    _patch_u64(b, m.nnz, m.nnz + (1 << 39), first + 8)
+    f = tmp_path / "ir.h5"
+    f.write_bytes(bytes(b))
+    rc = native.dimgpu_h5_read_matlab_compatible(_b(f), b"A", rp.ctypes.data, ci.ctypes.data, v.ctypes.data)
+    assert rc == N.ERR_IO
+    msg = native.dimgpu_last_error_string()
+    assert b"expected" in msg or b"fewer bytes" in msg or b"host's memory" in msg, msg
+
+    # the vector claims 2^40 elements: longer than its stored bytes and than the host's memory
+    b = bytearray(raw)
+    _patch_u64(b, 77, 1 << 40, 0)
+    f = tmp_path / "y.h5"
+    f.write_bytes(bytes(b))
+    n = ctypes.c_uint64()
+    assert native.dimgpu_h5_vector_length(_b(f), b"Y", ctypes.byref(n)) == N.ERR_IO
+    out = np.zeros(77)
+    assert native.dimgpu_h5_read_vector(_b(f), b"Y", out.ctypes.data) == N.ERR_IO
+
+    # a dataspace whose dimensions multiply past 64 bits
+    b = bytearray(raw)
+    at = _patch_u64(b, 77, 1 << 62, 0)
+    f = tmp_path / "ovf.h5"
+    f.write_bytes(bytes(b))
+    assert native.dimgpu_h5_vector_length(_b(f), b"Y", ctypes.byref(n)) == N.ERR_IO
+
+
+def test_corrupted_files_return_errors(native, tmp_path, monkeypatch):
+    """Truncations and random byte changes of a contiguous and a chunked, compressed file (fixed seed): every
+    read returns OK or an error code -- never out of memory, never a crash."""
+    import random
+
+    rng = np.random.default_rng(5)
+    m = random_csr(rng, 120, 100, 4.0, empty_frac=0.1)
+    y = rng.uniform(-1, 1, 300)
+    bases = []
+    for form in (None, "dynamic"):
+        p = tmp_path / f"base_{form}.h5"
+        if form:
+            monkeypatch.setattr(h5, "_write_dataset", _chunked_writer(**CHUNKED[form]))
+        h5.write_matlab_compatible(p, "A", m)
+        h5.write_vector(p, "Y", y)
+        monkeypatch.undo()
+        bases.append(p.read_bytes())
+    rnd = random.Random(7)
+    cases = []
+    for raw in bases:
+        cases += [raw[:k] for k in range(0, len(raw), max(1, len(raw) // 60))]
+        for _ in range(250):
+            b = bytearray(raw)
+            lim = min(len(b), 2048) if rnd.random() < 0.7 else len(b)
+            for _ in range(rnd.randint(1, 4)):
+                i = rnd.randrange(lim)
+                b[i] = rnd.randrange(256) if rnd.random() < 0.5 else b[i] ^ (1 << rnd.randrange(8))
+            cases.append(bytes(b))
+    rows, cols, nnz, n = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_uint64()
+    f = tmp_path / "case.h5"
+    allowed = {N.OK, N.ERR_IO, N.ERR_INVALID_ARGUMENT}
+    for raw in cases:
+        f.write_bytes(raw)
+        rc = native.dimgpu_h5_csr_dimensions(_b(f), b"A", ctypes.byref(rows), ctypes.byref(cols), ctypes.byref(nnz))
+        assert rc in allowed
+        if rc == N.OK:
+            assert rows.value < (1 << 20) and nnz.value < (1 << 20)  # the sizes come from intact metadata
+            rp = np.zeros(rows.value + 1, np.uint32)
+            ci = np.zeros(nnz.value, np.uint32)
+            v = np.zeros(nnz.value)
+            rc = native.dimgpu_h5_read_matlab_compatible(_b(f), b"A", rp.ctypes.data, ci.ctypes.data, v.ctypes.data)
+            assert rc in allowed
+        rc = native.dimgpu_h5_vector_length(_b(f), b"Y", ctypes.byref(n))
+        assert rc in allowed
+        if rc == N.OK and n.value < (1 << 20):
+            out = np.zeros(n.value)
+            assert native.dimgpu_h5_read_vector(_b(f), b"Y", out.ctypes.data) in allowed

@@ -103,6 +103,9 @@ def test_round_trip_of_the_writer(native, tmp_path):
     ("%%MatrixMarket matrix coordinate real general\n2 2 1\n3 1 1.0\n", N.ERR_INVALID_ARGUMENT, b"out of range"),
     ("%%MatrixMarket matrix coordinate real general\n2 2 1\n0 1 1.0\n", N.ERR_INVALID_ARGUMENT, b"out of range"),
     ("%%MatrixMarket matrix coordinate real general\n2 2 1\n1 1 x\n", N.ERR_INVALID_ARGUMENT, b"not a number"),
+    # a size line that would size the arrays far past what the file can hold is refused before allocating
+    ("%%MatrixMarket matrix coordinate real general\n3 3 1000000000000\n1 1 1.0\n", N.ERR_INVALID_ARGUMENT,
+     b"more entries than the file holds"),
 ])
 def test_errors(native, tmp_path, text, code, msg):
     p = tmp_path / "bad.mtx"
@@ -113,3 +116,31 @@ def test_errors(native, tmp_path, text, code, msg):
 
 def test_missing_file(native, tmp_path):
     assert _c_load(native, tmp_path / "missing.mtx") == N.ERR_IO
+
+
+def test_corrupted_files_return_errors(native, tmp_path):
+    """Random byte changes and truncations of a symmetric file (fixed seed): every read returns OK or an
+    error code, and a successful read has no more entries than the file can hold."""
+    import random
+
+    p = tmp_path / "s.mtx"
+    _write(p, CASES["symmetric"][0], "400 400 3000",
+           _random_entries(np.random.default_rng(1), 400, 400, 3000, lower=True))
+    raw = p.read_bytes()
+    rnd = random.Random(3)
+    f = tmp_path / "case.mtx"
+    allowed = {N.OK, N.ERR_INVALID_ARGUMENT, N.ERR_IO}
+    cases = [raw[:k] for k in range(0, len(raw), len(raw) // 40)]
+    for _ in range(300):
+        b = bytearray(raw)
+        lim = 200 if rnd.random() < 0.5 else len(b)
+        for _ in range(rnd.randint(1, 4)):
+            b[rnd.randrange(lim)] = rnd.choice(b"0123456789 \n%.-eE9")
+        cases.append(bytes(b))
+    for c in cases:
+        f.write_bytes(c)
+        r = _c_load(native, f)
+        if isinstance(r, int):
+            assert r in allowed
+        else:
+            assert r.nnz <= 2 * len(c)
