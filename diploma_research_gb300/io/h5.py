@@ -24,6 +24,7 @@ where this was built, so interoperability with them is by construction, not by t
 """
 from __future__ import annotations
 
+import math
 import mmap
 import os
 import struct
@@ -66,7 +67,7 @@ def _dt_float(size: int) -> bytes:
 
 
 def _dt_array(base: bytes, base_size: int, dims) -> bytes:
-    n = int(np.prod(dims))
+    n = math.prod(dims)
     props = struct.pack("<B3x", len(dims)) + b"".join(struct.pack("<I", d) for d in dims)
     props += b"".join(struct.pack("<I", i) for i in range(len(dims)))  # permutation (version 2)
     return struct.pack("<BBBBI", 0x2A, 0, 0, 0, base_size * n) + props + base
@@ -269,9 +270,28 @@ def _parse_type(b: bytes, p: int) -> tuple[_Type, int]:
         if ver < 3:
             q += 4 * nd  # permutation indices
         base, q = _parse_type(b, q)
-        n = int(np.prod(dims))
+        n = math.prod(dims)
         return _Type(base.kind, size, base.size, n), q
     raise H5FormatError(f"datatype class {cls} is not supported")
+
+
+def _host_memory() -> int | None:
+    try:
+        return os.sysconf("SC_PHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
+    except (AttributeError, ValueError, OSError):
+        return None
+
+
+def _check_extent(nbytes: int, layout: bytes) -> None:
+    """Sizes read from a file are checked before they size an allocation: no dataset larger than the host's
+    memory, and a contiguous dataset must store as many bytes as its dataspace holds."""
+    mem = _host_memory()
+    if mem is not None and nbytes > mem:
+        raise H5FormatError(f"dataset of {nbytes} bytes exceeds the host's memory")
+    if layout[1] == 1:
+        a, sz = struct.unpack_from("<QQ", layout, 2)
+        if a != UNDEF and sz < nbytes:
+            raise H5FormatError("contiguous dataset stores fewer bytes than its dataspace holds")
 
 
 def _parse_space(b: bytes, p: int) -> tuple:
@@ -387,7 +407,7 @@ class _File:
             p += rnd(tsz)
             shape = _parse_space(d, p)
             p += rnd(ssz)
-            n = int(np.prod(shape)) if shape else 1
+            n = math.prod(shape) if shape else 1
             val = np.frombuffer(d, typ.numpy(), n * max(1, typ.inner), p)
             out[name] = val[0] if n == 1 and not typ.inner else val.copy()
         return out
@@ -410,6 +430,7 @@ class _File:
             raise ValueError(f"slab [{start}, {start + count}) of a dataset of {n}")
         per = typ.size * max(1, typ.inner) if typ.inner else typ.size
         if len(shape) == 1 and layout[0] == 3 and layout[1] == 1 and not typ.inner:
+            _check_extent(n * per, layout)
             a, sz = struct.unpack_from("<QQ", layout, 2)
             if a == UNDEF:
                 return np.zeros(count, typ.numpy())
@@ -432,10 +453,11 @@ class _File:
                 filters = self._filters(d)
         if typ is None or shape is None or layout is None:
             raise H5FormatError("not a dataset")
-        count = int(np.prod(shape)) if shape else 1
+        count = math.prod(shape) if shape else 1
         nbytes = count * typ.size
         if layout[0] != 3:
             raise H5FormatError(f"layout message version {layout[0]}")
+        _check_extent(nbytes, layout)
         cls = layout[1]
         if cls == 0:  # compact
             sz = struct.unpack_from("<H", layout, 2)[0]
@@ -477,7 +499,7 @@ class _File:
         if nd != 2:
             raise H5FormatError("only 1-D chunked datasets are supported")
         chunk_elems = cdims[0]
-        count = int(np.prod(shape))
+        count = math.prod(shape)
         out = bytearray(count * typ.size)
         b = self.b
         for f in filters:

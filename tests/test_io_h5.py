@@ -165,3 +165,19 @@ def test_reader_chunked_datasets(tmp_path, monkeypatch, deflate):
     h5.write_vector(p, "Y", data, append=False)
     monkeypatch.undo()
     assert np.array_equal(h5.read_vector(p, "Y"), data)
+
+
+def test_reader_refuses_oversized_dataspaces(tmp_path):
+    """A dataspace claiming more elements than its contiguous storage holds, or than the host's memory,
+    is a format error before anything is allocated; dimensions whose product passes 64 bits as well."""
+    p = tmp_path / "y.h5"
+    h5.write_vector(p, "Y", np.arange(77.0))
+    raw = p.read_bytes()
+    for claim in (78, 1 << 40, 1 << 63):
+        b = bytearray(raw)
+        at = bytes(b).find(struct.pack("<Q", 77))
+        b[at:at + 8] = struct.pack("<Q", claim)
+        bad = tmp_path / f"bad_{claim}.h5"
+        bad.write_bytes(bytes(b))
+        with pytest.raises(h5.H5FormatError):
+            h5.read_vector(bad, "Y")
