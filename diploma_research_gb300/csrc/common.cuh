@@ -219,19 +219,6 @@ __device__ __forceinline__ float ldg_x_stream(const float* p, uint64_t policy) {
     return v;
 }
 
-// Coherent loads of data that the same (persistent) kernel wrote earlier, after a grid barrier: no
-// read-only path, and volatile so that the compiler never merges loads across loop iterations.
-__device__ __forceinline__ double ldc_x(const double* p, uint64_t policy) {
-    double v;
-    asm volatile("ld.global.L1::evict_last.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(policy));
-    return v;
-}
-__device__ __forceinline__ float ldc_x(const float* p, uint64_t policy) {
-    float v;
-    asm volatile("ld.global.L1::evict_last.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(policy));
-    return v;
-}
-
 // Stores that the next kernel will read: kept in L2 by `policy`.
 __device__ __forceinline__ void st_keep(double* p, double v, uint64_t policy) {
     asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(v), "l"(policy) : "memory");

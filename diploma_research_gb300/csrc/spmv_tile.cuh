@@ -106,33 +106,27 @@ struct tile_io {
     uint32_t rows;
 };
 
-// How the x gathers load: the read-only path kept in L1 (matrices whose column indices have locality),
-// the read-only path without L1 allocation (no locality), or coherent loads for the persistent CG
-// kernel, which rewrites x between its SpMV phases.
-enum : int { kXReadOnly = 0, kXCoherent = 1, kXStream = 2 };
+// How the x gathers load: the read-only path kept in L1 (matrices whose column indices have locality)
+// or the read-only path without L1 allocation (no locality).  The values name the kernels' template
+// argument.
+enum : int { kXReadOnly = 0, kXStream = 2 };
 
 template <int XM, typename VT>
 __device__ __forceinline__ VT load_x(const VT* p, uint64_t policy) {
-    if constexpr (XM == kXCoherent)
-        return ldc_x(p, policy);
-    else if constexpr (XM == kXStream)
+    if constexpr (XM == kXStream)
         return ldg_x_stream(p, policy);
     else
         return ldg_x(p, policy);
 }
 
 // Writes a row the chain closed (lane 0) and accumulates its share of x.y.
-template <typename VT, bool DOT, int XM = kXReadOnly>
+template <typename VT, bool DOT>
 __device__ __forceinline__ void chain_write_row(const tile_io<VT>& io, warp_chain<VT>& ch, unsigned lane,
                                                 uint32_t row, VT val) {
     if (lane == 0) {
         io.y[row] = val;
-        if constexpr (DOT) {
-            if constexpr (XM == kXCoherent)
-                ch.dot_acc += (double)val * (double)ldc_x(io.x + row, policy_evict_last());
-            else
-                ch.dot_acc += (double)val * (double)ldg_keep(io.x + row);
-        }
+        if constexpr (DOT)
+            ch.dot_acc += (double)val * (double)ldg_keep(io.x + row);
     }
 }
 
@@ -161,7 +155,7 @@ __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned cha
     VT xrow = VT(0);
     if constexpr (DOT) {
         if (row_start + lane < io.rows)
-            xrow = load_x<XM == kXCoherent ? kXCoherent : kXReadOnly>(io.x + row_start + lane, pol_keep);
+            xrow = load_x<kXReadOnly>(io.x + row_start + lane, pol_keep);
     }
     const uint32_t flag = (uint32_t)((uint64_t(w) >> (G::F.yb + G::F.sb)) & G::FMASK);
     const bool capped = (__shfl_sync(kFull, flag, 0) & 1u) != 0;
@@ -266,7 +260,7 @@ __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned cha
     if (K == 1) {
         if (capped) {
             if (ch.open)
-                chain_write_row<VT, DOT, XM>(io, ch, lane, ch.carry_row, ch.carry);
+                chain_write_row<VT, DOT>(io, ch, lane, ch.carry_row, ch.carry);
             ch.open = true;
             ch.carry = H;
             ch.carry_row = row_start;
@@ -280,7 +274,7 @@ __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned cha
     } else {
         if (capped || ch.open) {
             if (capped && ch.open)
-                chain_write_row<VT, DOT, XM>(io, ch, lane, ch.carry_row, ch.carry);
+                chain_write_row<VT, DOT>(io, ch, lane, ch.carry_row, ch.carry);
             if (!capped && lane == 0)
                 ystage[0] = ch.carry + H;  // the row that began before this tile closes here
             head_staged = true;
@@ -306,7 +300,7 @@ __device__ __forceinline__ void process_tile(const tile_io<VT>& io, unsigned cha
             st_keep(io.y + row, val, pol_keep);
             if constexpr (DOT) {
                 const bool have = !dirty && j == lo + lane && lane + lo < 32;
-                const VT xr = have ? xfirst : load_x<XM == kXCoherent ? kXCoherent : kXReadOnly>(io.x + row, pol_keep);
+                const VT xr = have ? xfirst : load_x<kXReadOnly>(io.x + row, pol_keep);
                 ch.dot_acc = fma((double)val, (double)xr, ch.dot_acc);
             }
         }
