@@ -51,10 +51,6 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 
-__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
-    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
 __device__ __forceinline__ void fence_mbar_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
@@ -192,8 +188,6 @@ __device__ __forceinline__ float ldg_keep<float>(const float* p) {
     return v;
 }
 
-__device__ __forceinline__ uint32_t ldg_u32(const uint32_t* p) { return __ldg(p); }
-
 // Gathered-vector loads: read-only path, kept in L1 and (by `policy`) in L2.
 __device__ __forceinline__ double ldg_x(const double* p, uint64_t policy) {
     double v;
@@ -227,17 +221,13 @@ __device__ __forceinline__ void st_keep(float* p, float v, uint64_t policy) {
     asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(policy) : "memory");
 }
 
-// 16-byte vector loads/stores of the CG vectors with an L2 policy.  The loads carry no memory
+// 16-byte vector loads of the CG vectors with an L2 policy.  The loads carry no memory
 // clobber so that independent loads can be batched; callers never load an element after storing it
 // in the same kernel.
 __device__ __forceinline__ double2 ld2_keep(const double* p, uint64_t policy) {
     double2 v;
     asm("ld.global.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(p), "l"(policy));
     return v;
-}
-__device__ __forceinline__ void st2_keep(double* p, double2 v, uint64_t policy) {
-    asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;" ::"l"(p), "d"(v.x), "d"(v.y), "l"(policy)
-                 : "memory");
 }
 // Stores of streamed vector elements that order nothing else: volatile (never dropped) but without a
 // memory clobber, so the compiler may issue the next elements' loads ahead of them.
@@ -255,18 +245,11 @@ __device__ __forceinline__ float4 ld4_keep(const float* p, uint64_t policy) {
                  : "l"(p), "l"(policy));
     return v;
 }
-__device__ __forceinline__ void st4_keep(float* p, float4 v, uint64_t policy) {
-    asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z),
-                 "f"(v.w), "l"(policy)
-                 : "memory");
-}
 
 // ------------------------------------------------------------------------------------------------
 // Warp helpers.
 // ------------------------------------------------------------------------------------------------
 constexpr unsigned kFull = 0xffffffffu;
-
-__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
