@@ -180,6 +180,8 @@ csr_host load_as_csr(const char* path) {
     const uint64_t rows = parse_index(ss.token()), cols = parse_index(ss.token()), nnz = parse_index(ss.token());
     if (rows > 0xFFFFFFFFull || cols > 0xFFFFFFFFull)
         throw std::invalid_argument("matrix dimensions must fit in 32 bits");
+    if (symmetric && rows != cols)  // each entry's mirror (col, row) must be a row of the matrix
+        throw std::invalid_argument("a symmetric or Hermitian matrix must be square");
     // the size line sizes the allocations below: an entry takes at least four bytes ("1 1\n"), and the row
     // arrays must fit in the host's memory
     if (nnz > f.size() / 4)

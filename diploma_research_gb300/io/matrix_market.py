@@ -41,6 +41,8 @@ def load_as_coo(path) -> coo:
         while line and (line.startswith("%") or not line.strip()):
             line = fh.readline()
         rows, cols, nnz = (int(t) for t in line.split()[:3])
+        if symm in ("symmetric", "hermitian") and rows != cols:  # the mirror (col, row) must be a row
+            raise ValueError("a symmetric or Hermitian matrix must be square")
         pattern = field == "pattern"
         ncol = 2 if pattern else 3
         data = np.loadtxt(fh, dtype=np.float64, ndmin=2, max_rows=nnz) if nnz else np.zeros((0, ncol))

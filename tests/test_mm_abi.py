@@ -103,6 +103,9 @@ def test_round_trip_of_the_writer(native, tmp_path):
     ("%%MatrixMarket matrix coordinate real general\n2 2 1\n3 1 1.0\n", N.ERR_INVALID_ARGUMENT, b"out of range"),
     ("%%MatrixMarket matrix coordinate real general\n2 2 1\n0 1 1.0\n", N.ERR_INVALID_ARGUMENT, b"out of range"),
     ("%%MatrixMarket matrix coordinate real general\n2 2 1\n1 1 x\n", N.ERR_INVALID_ARGUMENT, b"not a number"),
+    # a symmetric matrix that is not square: an entry's mirror would lie outside the rows
+    ("%%MatrixMarket matrix coordinate real symmetric\n2 3 1\n1 3 1.0\n", N.ERR_INVALID_ARGUMENT, b"square"),
+    ("%%MatrixMarket matrix coordinate real hermitian\n50 90 1\n22 58 1.0\n", N.ERR_INVALID_ARGUMENT, b"square"),
     # a size line that would size the arrays far past what the file can hold is refused before allocating
     ("%%MatrixMarket matrix coordinate real general\n3 3 1000000000000\n1 1 1.0\n", N.ERR_INVALID_ARGUMENT,
      b"more entries than the file holds"),
@@ -112,6 +115,13 @@ def test_errors(native, tmp_path, text, code, msg):
     p.write_text(text)
     assert _c_load(native, p) == code
     assert msg in native.dimgpu_last_error_string()
+
+
+def test_python_reader_refuses_a_non_square_symmetric_file(tmp_path):
+    p = tmp_path / "ns.mtx"
+    p.write_text("%%MatrixMarket matrix coordinate real symmetric\n2 3 1\n1 3 1.0\n")
+    with pytest.raises(ValueError, match="square"):
+        mm.load_as_csr(str(p))
 
 
 def test_missing_file(native, tmp_path):
