@@ -139,6 +139,44 @@ def test_oracle_bitexact_vs_live_reference(seed):
     assert np.array_equal(o.spmv(x, nthreads=oracle.RefCSR5.max_threads()), R.spmv(x))
 
 
+STRUCTURED = {
+    # nnz an exact multiple of the 64-element tile: no CSR tail
+    "no_tail": [16] * 40,
+    # rows of exactly sigma elements, each row one tile column
+    "sigma_rows": [16] * 37 + [5],
+    # rows of exactly one tile, and a row of one tile plus one element
+    "tile_rows": [64] * 9 + [65, 63, 1],
+    # one row spanning every thread's chunk, between short rows
+    "row_across_threads": [3, 2] + [4000] + [1, 7, 2],
+    # empty rows at the edges of tiles and after the last tile (the tail holds only empty rows)
+    "empty_at_edges": ([0, 32, 0, 32, 0] * 10) + [0, 0, 0],
+    # a lone tail row after full tiles
+    "lone_tail_row": [64] * 6 + [3],
+    # every row empty but one dense row at the very end
+    "dense_last_row": [0] * 300 + [700],
+}
+
+
+@pytest.mark.skipif(oracle.ref() is None, reason="reference shim not buildable on this host")
+@pytest.mark.parametrize("case", sorted(STRUCTURED))
+def test_oracle_bitexact_vs_live_reference_structured(case):
+    """Shapes at the format's boundaries, against the reference's own compiled conversion and SpMV."""
+    rng = np.random.default_rng(len(case))
+    lens = STRUCTURED[case]
+    m = csr_from_lengths(lens, max(5000, max(lens) + 1), rng)
+    rows, cols = m.dimensions.rows, m.dimensions.cols
+    o = _oracle_of(rows, cols, m.row_start_offsets, m.col_indices, m.values)
+    R = oracle.RefCSR5(rows, cols, m.row_start_offsets, m.col_indices, m.values)
+    e = R.export()
+    assert np.array_equal(o.tile_ptr, e["tile_ptr"])
+    assert np.array_equal(o.tile_desc.astype(np.uint32), e["tile_desc"])
+    assert np.array_equal(o.tile_desc_offset_ptr, e["tile_desc_offset_ptr"])
+    assert np.array_equal(o.tile_desc_offset, e["tile_desc_offset"])
+    assert np.array_equal(o.vals, e["vals"]) and np.array_equal(o.col_idx, e["col_idx"])
+    x = rng.uniform(-1, 1, cols)
+    assert np.array_equal(o.spmv(x, nthreads=oracle.RefCSR5.max_threads()), R.spmv(x))
+
+
 @pytest.mark.skipif(oracle.ref() is None, reason="reference shim not buildable on this host")
 def test_oracle_cg_vs_live_reference():
     from diploma_research_gb300.generators import laplacian_2d_5pt, rhs
